@@ -1,0 +1,384 @@
+"""Benchmark of the GB300 path-tracing core.
+
+Headline (the intersection microbench): closest-hit queries of 2^24 rays (origins uniform
+in the scene box, directions uniform on the sphere, tmax = 1e6) against a 10,485,760-
+triangle soup of 2^20 instances x 10 triangles built with the reference's BVH algorithm.
+  value   Grays/s with rays and hits resident in HBM (CUDA events on the launching stream)
+  e2e     the same through lf_trace_closest with page-locked host buffers: every step copies
+          the rays in and the hits out
+Secondary numbers (reported under "extra"): progressive renders of the Cornell box
+(256^2, 64 spp, depth 4) and of the 13-icosphere ~1.06M-triangle scene (1920x1080,
+16 spp, depth 8) in Msamples/s and extension rays/s.
+
+`--impl reference` times the CPU restatement of the reference traversal (the reference's
+own GPU path is an OpenGL shader and cannot run here) on the host cores.
+Multi-GPU: replicas only - every rank runs the full workload on its own GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instances-log2", type=int, default=20)
+    ap.add_argument("--rays-log2", type=int, default=24)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as td
+
+        td.init_process_group("gloo", init_method="env://")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+
+        td.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as td
+
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_soup(inst_log2):
+    import lavaframe_gb300 as lf
+
+    t = time.time()
+    s = lf.HostScene().gen_soup(1 << inst_log2, 10, 1)
+    t_gen = time.time() - t
+    t = time.time()
+    s.build()
+    t_build = time.time() - t
+    return s, t_gen, t_build
+
+
+def soup_rays(s, n):
+    import lavaframe_gb300 as lf
+
+    a = s.view()
+    nodes = np.ctypeslib.as_array(a.nodes, shape=(a.num_nodes * 9,)).reshape(-1, 9)
+    root = nodes[a.top_level_index]
+    return lf.gen_rays(root[0:3], root[3:6], n, 2), root
+
+
+def algorithmic_bytes_per_ray(stats, nrays):
+    """Reference data model: 32 B ray + 16 B hit, 36 B per node box tested (two per inner
+    node visit), 60 B per triangle test (12 B indices + 3 x 16 B vertices), 64 B per
+    instance entered (its transform)."""
+    inner, tris, inst = float(stats[0]), float(stats[1]), float(stats[4])
+    return 32.0 + 16.0 + (36.0 * 2.0 * inner + 60.0 * tris + 64.0 * inst) / nrays
+
+
+def cpu_baseline(view, rays, target_s, cull_abs):
+    import oracle
+
+    threads = os.cpu_count() or 1
+    n = min(len(rays), 1 << 16)
+    t = time.time()
+    _, st = oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    dt = max(time.time() - t, 1e-3)
+    m = int(min(len(rays), max(n, n * target_s / dt)))
+    m = max(n, (m // n) * n)
+    t = time.time()
+    _, st = oracle.trace_closest(view, rays[:m], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    dt = time.time() - t
+    return m / dt / 1e9, threads, m, dt, st
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import lavaframe_gb300 as lf  # host scene layer only (BVH build), no GPU
+    import oracle
+
+    from lavaframe_gb300 import build as b
+    b.build_core()
+    b.build_oracle()
+    s, _, _ = build_soup(args.instances_log2)
+    rays, root = soup_rays(s, 1 << args.rays_log2)
+    extent = float(np.abs(root[:6]).max())
+    cull_abs = 64 * float(np.spacing(np.float32(extent)))
+    view = s.view()
+    threads = os.cpu_count() or 1
+    n = min(len(rays), 1 << 16)
+    t = time.time()
+    oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    per = (time.time() - t) / n
+    sample = int(min(len(rays), max(n, 6.0 / max(per, 1e-9))))
+    sample = max(n, (sample // n) * n)
+    for i in range(args.warmup):
+        oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    times = []
+    for i in range(args.steps):
+        off = (i * sample) % max(1, len(rays) - sample + 1)
+        t = time.time()
+        oracle.trace_closest(view, rays[off:off + sample], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+        times.append(time.time() - t)
+    total = sum(times)
+    v = sample * args.steps / total / 1e9
+    line = {
+        "impl": "reference", "metric": "closest-hit Grays/s (intersection microbench)", "value": v, "unit": "Grays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"intersection microbench: {1 << args.instances_log2} instances x 10 triangles, "
+                               f"2^{args.rays_log2} rays (each step a {sample}-ray sample)",
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "Grays/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} rays per step of the 2^{args.rays_log2}-ray set"},
+        "e2e": {"value": v, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference traces in an OpenGL fragment shader that cannot run on this host; "
+                "this arm times the scalar C++ restatement of its traversal on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def render_extra(ctx, which):
+    import lavaframe_gb300 as lf
+
+    if which == "c1":
+        s = lf.HostScene().gen_cornell(256, 256).build()
+        spp = 64
+    else:
+        s = lf.HostScene().gen_icospheres(13, 6, 3, 1024, 512).build()
+        spp = 16
+    p = s.render_params()
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p)
+    f.render(0, 1)
+    f.sync()
+    f.reset()
+    ctx.timer_start()
+    f.render(0, spp)
+    ms = ctx.timer_stop()
+    f.sync()
+    ctr = f.counters()
+    out = {"Msamples_per_s": ctr[0] / (ms / 1e3) / 1e6, "ext_rays_per_s": ctr[1] / (ms / 1e3),
+           "shadow_rays_per_s": ctr[2] / (ms / 1e3), "ms": ms, "spp": spp,
+           "resolution": [p.width, p.height], "max_depth": p.max_depth,
+           "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1])}
+    f.close()
+    ds.close()
+    return out
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        barrier(world)
+        return
+
+    import lavaframe_gb300 as lf
+    from lavaframe_gb300 import build as b
+
+    b.build_core()
+    b.build_oracle()
+    ctx = lf.Context(local)
+    s, t_gen, t_build = build_soup(args.instances_log2)
+    nrays = 1 << args.rays_log2
+    rays, root = soup_rays(s, nrays)
+    ds = ctx.upload(s)
+    L = lf.lib()
+    import ctypes as C
+
+    # device-resident inputs
+    d_rays, d_hits = C.c_void_p(), C.c_void_p()
+    ctx._c(L.lf_device_alloc(ctx.h, rays.nbytes, C.byref(d_rays)))
+    ctx._c(L.lf_device_alloc(ctx.h, nrays * 16, C.byref(d_hits)))
+    ctx._c(L.lf_copy_to_device(ctx.h, d_rays, rays.ctypes.data_as(C.c_void_p), rays.nbytes))
+
+    for _ in range(args.warmup):
+        ctx._c(L.lf_trace_closest_device(ctx.h, ds.h, d_rays, nrays, d_hits, 0))
+    ctx.sync()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        ctx.timer_start()
+        for _ in range(args.steps):
+            ctx._c(L.lf_trace_closest_device(ctx.h, ds.h, d_rays, nrays, d_hits, 0))
+        ms = ctx.timer_stop()
+        ctx.sync()
+    barrier(world)
+    ms = max_over_ranks(world, ms)
+    value = world * nrays * args.steps / (ms / 1e3) / 1e9
+
+    # end to end: page-locked host rays in, hits out, every step
+    h_rays, h_hits = C.c_void_p(), C.c_void_p()
+    ctx._c(L.lf_host_alloc(ctx.h, rays.nbytes, C.byref(h_rays)))
+    ctx._c(L.lf_host_alloc(ctx.h, nrays * 16, C.byref(h_hits)))
+    C.memmove(h_rays, rays.ctypes.data, rays.nbytes)
+    fr = C.cast(h_rays, C.POINTER(C.c_float))
+    for _ in range(args.warmup):
+        ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, nrays, h_hits, 0))
+    barrier(world)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, nrays, h_hits, 0))
+    e2e_s = time.perf_counter() - t
+    barrier(world)
+    e2e_s = max_over_ranks(world, e2e_s)
+    e2e = world * nrays * args.steps / e2e_s / 1e9
+    hits = np.frombuffer((C.c_char * (nrays * 16)).from_address(h_hits.value), dtype=lf.HIT_DTYPE).copy()
+
+    # traversal counts for the algorithmic bytes (device counters, same visit order as the oracle)
+    n_stats = min(nrays, 1 << 20)
+    ctx.trace_closest(ds, rays[:n_stats], flags=lf.TRACE_STATS)
+    dstats = ctx.trace_stats()
+    extra = {}
+    if rank == 0:
+        import oracle
+
+        extent = float(np.abs(root[:6]).max())
+        cull_abs = 64 * float(np.spacing(np.float32(extent)))
+        cpu_v, cores, sample, cpu_dt, ostats = cpu_baseline(s.view(), rays, args.cpu_seconds, cull_abs)
+        # spot check: the sampled rays agree with the oracle bit for bit
+        ref_hits, _ = oracle.trace_closest(s.view(), rays[:4096], cull_rel=1e-4, cull_abs=cull_abs)
+        extra["parity_spot_check_4096_rays"] = bool(ref_hits.tobytes() == hits[:4096].tobytes())
+        bpr = algorithmic_bytes_per_ray(ostats, sample)
+        peak, peak_kind = measured_peaks()
+        launch_s = ms / 1e3 / args.steps
+        achieved = bpr * nrays / launch_s / 1e9
+        prof = ROOT / "profiles" / "c2_trace_closest_traffic.json"
+        traffic = None
+        if prof.exists():
+            pj = json.loads(prof.read_text())
+            traffic = pj.get("dram_bytes_per_ray", 0) * nrays
+        if not args.no_extras:
+            for w in ("c1", "c3_1m"):
+                try:
+                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3")
+                except Exception as e:  # reported, not fatal for the headline
+                    extra[w] = {"error": str(e)}
+        extra.update({"scene_build_s": t_build, "scene_generate_s": t_gen, "hit_fraction": float((hits["prim"] >= 0).mean()),
+                      "device_counters_per_ray": [x / n_stats for x in dstats],
+                      "oracle_counters_per_ray": [float(x) / sample for x in ostats],
+                      "algorithmic_bytes_per_ray": bpr, "scene_device_bytes": int(ds.device_bytes())})
+        line = {
+            "metric": "closest-hit Grays/s (intersection microbench)", "value": value, "unit": "Grays/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"intersection microbench: {1 << args.instances_log2} instances x 10 triangles "
+                                   f"({(1 << args.instances_log2) * 10} tris), 2^{args.rays_log2} rays, tmax 1e6",
+                       "rays": nrays, "triangles": (1 << args.instances_log2) * 10,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (rays 512 MiB + scene > 129 MB), no flush"},
+            "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": int(rays.nbytes),
+                    "d2h_bytes_per_step": int(nrays * 16)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "note": "algorithmic bytes of the reference data model per launch / CUDA-event launch time"},
+            "cpu_baseline": {"value": cpu_v, "unit": "Grays/s", "cores": cores, "kind": "port",
+                             "sample": f"{sample} of the 2^{args.rays_log2} rays, {cpu_dt:.1f} s"},
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "extra": extra,
+        }
+        print(json.dumps(line), flush=True)
+    barrier(world)
+    L.lf_host_free(ctx.h, h_rays)
+    L.lf_host_free(ctx.h, h_hits)
+    L.lf_device_free(ctx.h, d_rays)
+    L.lf_device_free(ctx.h, d_hits)
+    ds.close()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,255 @@
+/*
+ * lavaframe_gb300.h - C ABI of the GB300 path-tracing core for LavaFrame.
+ *
+ * This ABI replaces the OpenGL renderer boundary of the reference (the abstract
+ * LavaFrame::Renderer in LavaFrame/Renderer.h:71-117 and TiledRenderer in
+ * LavaFrame/TiledRenderer.h:15-72) and exposes the host scene layer (LavaFrame::Scene,
+ * LavaFrame/Scene.h:47-107) to non-C++ callers. Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every function returns lf_status (0 = LF_OK) unless stated otherwise; failures never
+ *    abort the process. The text of the last error is available from lf_ctx_last_error /
+ *    lf_hscene_last_error.
+ *  - The caller owns all host buffers; the library owns all device memory it allocates.
+ *  - One lf_ctx drives one GPU through one CUDA stream; calls on the same context are
+ *    serialised by an internal lock.
+ *  - Device-side failures (BVH stack overflow, step limit, queue overflow) are reported as
+ *    LF_ERR_DEVICE with the bits in lf_ctx_device_errors; no kernel traps or spins without
+ *    an iteration limit.
+ *  - Flat scene arrays use the reference layouts byte for byte: 36-byte BVH nodes
+ *    (bvh_translator.h:48-53), int3 triangle indices, float4 vertices/normals, 112-byte
+ *    materials (Material.h:13-77), 64-byte Mat4 transforms (row i = GL column i), 60-byte
+ *    lights (Scene.h:31-40), RGB32F environment with its marginal/conditional tables
+ *    (hdrloader.h:19-28), RGBA8 texture layers.
+ */
+#ifndef LAVAFRAME_GB300_H
+#define LAVAFRAME_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LF_ABI_VERSION 1
+
+typedef enum lf_status
+{
+    LF_OK = 0,
+    LF_ERR_INVALID = 1,    /* bad argument or inconsistent scene data */
+    LF_ERR_CUDA = 2,       /* CUDA runtime error (no device, launch failure, ...) */
+    LF_ERR_OOM = 3,        /* device allocation failed */
+    LF_ERR_DEVICE = 4,     /* a kernel reported an error bit (see lf_ctx_device_errors) */
+    LF_ERR_TIMEOUT = 5,    /* wait deadline passed; work is still in flight */
+    LF_ERR_STATE = 6,      /* call not valid in the object's current state */
+    LF_ERR_IO = 7,         /* file could not be read */
+    LF_ERR_BUDGET = 8      /* admission refused: memory budget exhausted */
+} lf_status;
+
+/* Device-side error bits. */
+#define LF_DEVERR_STACK 0x1u   /* BVH stack (64 entries) overflowed; the ray was ended */
+#define LF_DEVERR_STEPS 0x2u   /* traversal step limit reached */
+#define LF_DEVERR_QUEUE 0x4u   /* wavefront queue overflow */
+#define LF_DEVERR_INDEX 0x8u   /* out-of-range index caught by a device bounds check */
+
+typedef struct lf_ctx lf_ctx;
+typedef struct lf_scene lf_scene;     /* device-resident scene */
+typedef struct lf_frame lf_frame;     /* render target: accumulation + wavefront state */
+typedef struct lf_hscene lf_hscene;   /* host scene (LavaFrame::Scene) */
+
+/* ------------------------------------------------------------------ host scene
+ * Mirrors LavaFrame::Scene (Scene.h:47-107) and LoadSceneFromFile (Loader.h:15). */
+
+/* new Scene() */
+lf_status lf_hscene_create(lf_hscene** out);
+/* Scene::~Scene */
+void lf_hscene_destroy(lf_hscene* s);
+const char* lf_hscene_last_error(const lf_hscene* s);
+/* LoadSceneFromFile(filename, scene, renderOptions) (Loader.cpp:45-385); builds the
+ * acceleration structures like the reference. */
+lf_status lf_hscene_load_file(lf_hscene* s, const char* path);
+/* Scene::AddMesh (Scene.cpp:21-40) from memory: num_vertices = 3 x triangles, 4 floats
+ * each (xyz + u, xyz + v). Returns the mesh id, or -1. */
+int32_t lf_hscene_add_mesh(lf_hscene* s, const float* vertices_uvx, const float* normals_uvy, int32_t num_vertices);
+/* Scene::AddMesh(filename) with an OBJ file. Returns the mesh id, or -1. */
+int32_t lf_hscene_add_mesh_file(lf_hscene* s, const char* path);
+/* Scene::AddMaterial (Scene.cpp:70-75): 28 floats in Material order. Returns the id. */
+int32_t lf_hscene_add_material(lf_hscene* s, const float* material28);
+/* Scene::AddMeshInstance (Scene.cpp:92-97): transform = 16 floats (Mat4 data order). */
+int32_t lf_hscene_add_instance(lf_hscene* s, int32_t mesh_id, const float* transform16, int32_t material_id);
+/* Scene::AddLight (Scene.cpp:99-104): 15 floats in Light order. */
+int32_t lf_hscene_add_light(lf_hscene* s, const float* light15);
+/* Scene::AddCamera (Scene.cpp:15-19) plus the aperture/focal distance the loader sets. */
+lf_status lf_hscene_set_camera(lf_hscene* s, const float eye[3], const float lookat[3], float fov_degrees,
+                               float aperture, float focal_dist);
+/* Scene::AddHDR (Scene.cpp:77-90), from a Radiance .hdr file or from RGB32F memory. */
+lf_status lf_hscene_add_hdr_file(lf_hscene* s, const char* path);
+lf_status lf_hscene_add_hdr(lf_hscene* s, const float* rgb, int32_t width, int32_t height);
+/* Scene::CreateAccelerationStructures (Scene.cpp:180-231) - named ProcessScene in the
+ * build plan. Mesh-level builds run in parallel on `threads` host threads (0 = all). */
+lf_status lf_hscene_build(lf_hscene* s, int32_t threads);
+/* Scene::RebuildInstances (Scene.cpp:165-178) after editing instances. */
+lf_status lf_hscene_set_instance(lf_hscene* s, int32_t instance, const float* transform16, int32_t material_id);
+lf_status lf_hscene_rebuild_instances(lf_hscene* s);
+
+/* Pointers into the built scene, valid until the next build or destroy. */
+typedef struct lf_scene_view
+{
+    const float* nodes;            /* 9 floats per node */
+    int32_t num_nodes;
+    int32_t top_level_index;
+    const int32_t* vert_indices;   /* 3 ints per packed triangle */
+    int32_t num_tris;
+    const float* vertices_uvx;     /* 4 floats per vertex */
+    const float* normals_uvy;      /* 4 floats per vertex */
+    int32_t num_vertices;
+    const float* materials;        /* 28 floats per material */
+    int32_t num_materials;
+    const float* transforms;       /* 16 floats per instance */
+    int32_t num_instances;
+    const float* lights;           /* 15 floats per light */
+    int32_t num_lights;
+    const float* env_rgb;          /* width*height*3, may be NULL */
+    const float* env_marginal;     /* height*2 */
+    const float* env_conditional;  /* width*height*2 */
+    int32_t env_width, env_height;
+    const uint8_t* textures;       /* num_textures * tex_width * tex_height * 4 */
+    int32_t tex_width, tex_height, num_textures;
+} lf_scene_view;
+
+lf_status lf_hscene_view(const lf_hscene* s, lf_scene_view* out);
+
+/* Scene contents before flattening: counts[0..3] = meshes, instances, materials, lights.
+ * Optional arrays (may be NULL): vertex count per mesh, mesh id and material id per
+ * instance (Scene::meshes, Scene::meshInstances). */
+lf_status lf_hscene_counts(const lf_hscene* s, int32_t counts[4]);
+lf_status lf_hscene_layout(const lf_hscene* s, int32_t* mesh_vertex_counts, int32_t* instance_mesh,
+                           int32_t* instance_material);
+
+/* Per-render parameters: RenderOptions (Renderer.h:18-67), the Camera uniforms
+ * (TiledRenderer.cpp:506-520) and the RNG keying. */
+typedef struct lf_render_params
+{
+    int32_t width, height;
+    int32_t max_depth;
+    int32_t enable_rr, rr_depth;
+    int32_t use_env_map;       /* ENVMAP (requires environment data) */
+    int32_t use_constant_bg;   /* CONSTANT_BG */
+    float bg_color[3];
+    float hdr_multiplier;
+    float cam_position[3], cam_right[3], cam_up[3], cam_forward[3];
+    float cam_fov;             /* radians, as Camera::fov */
+    float cam_focal_dist, cam_aperture;
+    uint32_t seed;             /* 0 reproduces the reference's per-pixel seeding */
+    int32_t frame_base;        /* shader `frame` for sample 0; sample s uses frame_base + s */
+    int32_t tile_width, tile_height;   /* 0 = whole frame; else TiledRenderer tiling */
+} lf_render_params;
+
+/* Fills params from the scene's RenderOptions and camera. */
+lf_status lf_hscene_render_params(const lf_hscene* s, lf_render_params* out);
+
+/* Procedural workloads (seeded, deterministic on every host). */
+lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height);
+lf_status lf_gen_soup(lf_hscene* s, int32_t instances, int32_t tris_per_instance, uint64_t seed);
+lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint64_t seed, int32_t env_width,
+                            int32_t env_height);
+lf_status lf_gen_room(lf_hscene* s, int32_t boxes, uint64_t seed);
+/* Rays for the intersection microbench: origins uniform in [lo, hi], directions uniform on
+ * the sphere; 8 floats per ray (origin xyz, 0, direction xyz, tmax). */
+lf_status lf_gen_rays(const float lo[3], const float hi[3], int64_t n, uint64_t seed, float tmax, float* rays_out);
+
+/* ------------------------------------------------------------------ device context */
+lf_status lf_ctx_create(int32_t device, lf_ctx** out);
+void lf_ctx_destroy(lf_ctx* c);
+const char* lf_ctx_last_error(const lf_ctx* c);
+uint32_t lf_ctx_device_errors(const lf_ctx* c);
+lf_status lf_ctx_sync(lf_ctx* c);
+/* CUDA-event timing on the context stream: start records an event, stop records a second
+ * one, waits for it and returns the elapsed device time in milliseconds. */
+lf_status lf_ctx_timer_start(lf_ctx* c);
+lf_status lf_ctx_timer_stop(lf_ctx* c, float* ms);
+
+/* Renderer::Init upload set (Renderer.cpp:76-188): copies the flat arrays to HBM and
+ * re-encodes them for the kernels. */
+lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* view, lf_scene** out);
+/* Renderer::Update partial re-upload (Renderer.cpp:190-205): transforms, materials and
+ * the instance-level nodes from top_level_index on. */
+lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* view);
+lf_status lf_scene_release(lf_scene* sc);
+/* Culling margins of the traversal (relative, absolute); rel < 0 turns culling off. */
+lf_status lf_scene_set_culling(lf_scene* sc, float rel, float abs_margin);
+size_t lf_scene_device_bytes(const lf_scene* sc);
+
+/* ------------------------------------------------------------------ ray queries
+ * ClosestHit / AnyHit (closest_hit.glsl:7-205, anyhit.glsl:7-173) as batched queries.
+ * Ray: 8 floats (origin xyz, unused, direction xyz, tmax). tmax is the initial t of the
+ * closest-hit query (the shader uses INFINITY = 1e6) and maxDist of the any-hit query. */
+typedef struct lf_hit
+{
+    float t;          /* 1e6 when nothing was hit */
+    int32_t instance; /* instance index, -1 for none (or an analytic light hit) */
+    int32_t prim;     /* packed triangle index (row of vert_indices), -1 for none */
+    int32_t light;    /* analytic light index when a light is the closest hit, else -1 */
+} lf_hit;
+
+#define LF_TRACE_LIGHTS 0x1   /* include analytic lights, as the LIGHTS shader define */
+#define LF_TRACE_STATS 0x2    /* count node visits / triangle tests (slower) */
+
+/* Host buffers: copies rays in, traces, copies hits out (synchronous). */
+lf_status lf_trace_closest(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, lf_hit* hits, uint32_t flags);
+/* occluded[i] = 1 when something lies closer than tmax. */
+lf_status lf_trace_any(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, uint8_t* occluded, uint32_t flags);
+/* Device buffers, asynchronous on the context stream (lf_ctx_sync to wait). */
+lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_hits,
+                                  uint32_t flags);
+lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_occluded,
+                              uint32_t flags);
+/* Traversal counters of the last LF_TRACE_STATS query: node visits, triangle tests,
+ * leaf visits (sums over all rays). */
+lf_status lf_trace_stats(const lf_ctx* c, uint64_t out3[3]);
+
+/* Page-locked host memory (fast host<->device copies), e.g. for ray and hit buffers. */
+lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out);
+lf_status lf_host_free(lf_ctx* c, void* p);
+/* Device memory helpers for callers without their own allocator. */
+lf_status lf_device_alloc(lf_ctx* c, size_t bytes, void** out);
+lf_status lf_device_free(lf_ctx* c, void* p);
+lf_status lf_copy_to_device(lf_ctx* c, void* dst, const void* src, size_t bytes);
+lf_status lf_copy_to_host(lf_ctx* c, void* dst, const void* src, size_t bytes);
+
+/* ------------------------------------------------------------------ progressive render
+ * One render target with its accumulation buffer: TiledRenderer::Render/Update
+ * (TiledRenderer.cpp:317-554) without the GL passes. Samples accumulate in sample order,
+ * so results do not depend on how calls are batched. */
+#define LF_FRAME_FP64_ACCUM 0x1   /* also accumulate in double precision */
+#define LF_FRAME_USE_GRAPH 0x2    /* replay the bounce loop as a CUDA graph */
+#define LF_FRAME_TILED_FRAMES 0x4 /* TiledRenderer RNG keying: the shader `frame` advances per
+                                     tile (TiledRenderer.cpp:486-501): frame = frame_base +
+                                     sample * tiles + tile, tiles counted from the top row */
+
+lf_status lf_frame_create(lf_ctx* c, lf_scene* sc, const lf_render_params* p, uint32_t flags, lf_frame** out);
+/* Queue samples [first_sample, first_sample + count) (asynchronous). */
+lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count);
+/* Wait for queued work and report device errors. */
+lf_status lf_frame_sync(lf_frame* f);
+/* GetOutputBufferHDR (TiledRenderer.cpp:399-414): accumulated radiance sum, RGB32F,
+ * row 0 = bottom row as in GL. Divide by the sample count for the mean. */
+lf_status lf_frame_read_accum(lf_frame* f, float* rgb);
+lf_status lf_frame_read_accum64(lf_frame* f, double* rgb);
+/* Per-sample, per-pixel path radiance of the most recent batch, RGB32F,
+ * [sample][pixel], for path-level comparisons. */
+lf_status lf_frame_read_paths(lf_frame* f, float* rgb, int32_t max_samples);
+lf_status lf_frame_reset(lf_frame* f);
+/* Counters since creation/reset: [0] camera paths, [1] extension rays, [2] shadow rays,
+ * [3] light-index clamps (rand() == 1). */
+lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4]);
+/* Paths processed per wavefront batch (memory/parallelism trade-off); 0 = default. */
+lf_status lf_frame_set_batch(lf_frame* f, int32_t samples_per_batch);
+lf_status lf_frame_release(lf_frame* f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,421 @@
+"""GB300 path-tracing core for LavaFrame: Python bindings of the C ABI.
+
+The native library (liblfcore.so, built in-tree by `lavaframe_gb300.build`) holds the host
+scene layer (LavaFrame::Scene, BVH build and flatten, loader) and the sm_103a CUDA kernels.
+This module only marshals arguments through ctypes; there is no Python or CPU fallback for
+any GPU operation: if the library or a GPU is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "liblfcore.so"
+
+LF_OK = 0
+STATUS = {0: "LF_OK", 1: "LF_ERR_INVALID", 2: "LF_ERR_CUDA", 3: "LF_ERR_OOM", 4: "LF_ERR_DEVICE",
+          5: "LF_ERR_TIMEOUT", 6: "LF_ERR_STATE", 7: "LF_ERR_IO", 8: "LF_ERR_BUDGET"}
+TRACE_LIGHTS = 0x1
+TRACE_STATS = 0x2
+FRAME_FP64_ACCUM = 0x1
+FRAME_USE_GRAPH = 0x2
+FRAME_TILED_FRAMES = 0x4
+
+# symbol -> (restype, argtypes); kept in the same order as include/lavaframe_gb300.h
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int32)
+_SIG = {
+    "lf_hscene_create": (C.c_int, [C.POINTER(_P)]),
+    "lf_hscene_destroy": (None, [_P]),
+    "lf_hscene_last_error": (C.c_char_p, [_P]),
+    "lf_hscene_load_file": (C.c_int, [_P, C.c_char_p]),
+    "lf_hscene_add_mesh": (C.c_int32, [_P, _F, _F, C.c_int32]),
+    "lf_hscene_add_mesh_file": (C.c_int32, [_P, C.c_char_p]),
+    "lf_hscene_add_material": (C.c_int32, [_P, _F]),
+    "lf_hscene_add_instance": (C.c_int32, [_P, C.c_int32, _F, C.c_int32]),
+    "lf_hscene_add_light": (C.c_int32, [_P, _F]),
+    "lf_hscene_set_camera": (C.c_int, [_P, _F, _F, C.c_float, C.c_float, C.c_float]),
+    "lf_hscene_add_hdr_file": (C.c_int, [_P, C.c_char_p]),
+    "lf_hscene_add_hdr": (C.c_int, [_P, _F, C.c_int32, C.c_int32]),
+    "lf_hscene_build": (C.c_int, [_P, C.c_int32]),
+    "lf_hscene_set_instance": (C.c_int, [_P, C.c_int32, _F, C.c_int32]),
+    "lf_hscene_rebuild_instances": (C.c_int, [_P]),
+    "lf_hscene_view": (C.c_int, [_P, _P]),
+    "lf_hscene_counts": (C.c_int, [_P, _I]),
+    "lf_hscene_layout": (C.c_int, [_P, _I, _I, _I]),
+    "lf_hscene_render_params": (C.c_int, [_P, _P]),
+    "lf_gen_cornell": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "lf_gen_soup": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64]),
+    "lf_gen_icospheres": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.c_int32]),
+    "lf_gen_room": (C.c_int, [_P, C.c_int32, C.c_uint64]),
+    "lf_gen_rays": (C.c_int, [_F, _F, C.c_int64, C.c_uint64, C.c_float, _F]),
+    "lf_ctx_create": (C.c_int, [C.c_int32, C.POINTER(_P)]),
+    "lf_ctx_destroy": (None, [_P]),
+    "lf_ctx_last_error": (C.c_char_p, [_P]),
+    "lf_ctx_device_errors": (C.c_uint32, [_P]),
+    "lf_ctx_sync": (C.c_int, [_P]),
+    "lf_ctx_timer_start": (C.c_int, [_P]),
+    "lf_ctx_timer_stop": (C.c_int, [_P, _F]),
+    "lf_scene_upload": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "lf_scene_update_instances": (C.c_int, [_P, _P]),
+    "lf_scene_release": (C.c_int, [_P]),
+    "lf_scene_set_culling": (C.c_int, [_P, C.c_float, C.c_float]),
+    "lf_scene_device_bytes": (C.c_size_t, [_P]),
+    "lf_trace_closest": (C.c_int, [_P, _P, _F, C.c_int64, _P, C.c_uint32]),
+    "lf_trace_any": (C.c_int, [_P, _P, _F, C.c_int64, _P, C.c_uint32]),
+    "lf_trace_closest_device": (C.c_int, [_P, _P, _P, C.c_int64, _P, C.c_uint32]),
+    "lf_trace_any_device": (C.c_int, [_P, _P, _P, C.c_int64, _P, C.c_uint32]),
+    "lf_trace_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "lf_host_alloc": (C.c_int, [_P, C.c_size_t, C.POINTER(_P)]),
+    "lf_host_free": (C.c_int, [_P, _P]),
+    "lf_device_alloc": (C.c_int, [_P, C.c_size_t, C.POINTER(_P)]),
+    "lf_device_free": (C.c_int, [_P, _P]),
+    "lf_copy_to_device": (C.c_int, [_P, _P, _P, C.c_size_t]),
+    "lf_copy_to_host": (C.c_int, [_P, _P, _P, C.c_size_t]),
+    "lf_frame_create": (C.c_int, [_P, _P, _P, C.c_uint32, C.POINTER(_P)]),
+    "lf_frame_render": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "lf_frame_sync": (C.c_int, [_P]),
+    "lf_frame_read_accum": (C.c_int, [_P, _F]),
+    "lf_frame_read_accum64": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "lf_frame_read_paths": (C.c_int, [_P, _F, C.c_int32]),
+    "lf_frame_reset": (C.c_int, [_P]),
+    "lf_frame_counters": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "lf_frame_set_batch": (C.c_int, [_P, C.c_int32]),
+    "lf_frame_release": (C.c_int, [_P]),
+}
+
+
+class SceneView(C.Structure):
+    _fields_ = [("nodes", _F), ("num_nodes", C.c_int32), ("top_level_index", C.c_int32),
+                ("vert_indices", _I), ("num_tris", C.c_int32),
+                ("vertices_uvx", _F), ("normals_uvy", _F), ("num_vertices", C.c_int32),
+                ("materials", _F), ("num_materials", C.c_int32),
+                ("transforms", _F), ("num_instances", C.c_int32),
+                ("lights", _F), ("num_lights", C.c_int32),
+                ("env_rgb", _F), ("env_marginal", _F), ("env_conditional", _F),
+                ("env_width", C.c_int32), ("env_height", C.c_int32),
+                ("textures", C.POINTER(C.c_uint8)), ("tex_width", C.c_int32), ("tex_height", C.c_int32),
+                ("num_textures", C.c_int32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("max_depth", C.c_int32),
+                ("enable_rr", C.c_int32), ("rr_depth", C.c_int32), ("use_env_map", C.c_int32),
+                ("use_constant_bg", C.c_int32), ("bg_color", C.c_float * 3), ("hdr_multiplier", C.c_float),
+                ("cam_position", C.c_float * 3), ("cam_right", C.c_float * 3), ("cam_up", C.c_float * 3),
+                ("cam_forward", C.c_float * 3), ("cam_fov", C.c_float), ("cam_focal_dist", C.c_float),
+                ("cam_aperture", C.c_float), ("seed", C.c_uint32), ("frame_base", C.c_int32),
+                ("tile_width", C.c_int32), ("tile_height", C.c_int32)]
+
+
+HIT_DTYPE = np.dtype([("t", "<f4"), ("instance", "<i4"), ("prim", "<i4"), ("light", "<i4")])
+
+_lib = None
+
+
+def lib():
+    """Loads liblfcore.so (building it is `lavaframe_gb300.build.build_core`)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing; run lavaframe_gb300.build.build_core() first")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIG.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIG)
+
+
+class LFError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _fp(a):
+    return a.ctypes.data_as(_F)
+
+
+def _chk(st, msg_fn=lambda: ""):
+    if st != LF_OK:
+        raise LFError(st, msg_fn())
+
+
+class HostScene:
+    """LavaFrame::Scene through the C ABI (lf_hscene_*)."""
+
+    def __init__(self):
+        self.h = _P()
+        _chk(lib().lf_hscene_create(C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().lf_hscene_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self):
+        return lib().lf_hscene_last_error(self.h).decode()
+
+    def _c(self, st):
+        _chk(st, self.error)
+
+    def load_file(self, path):
+        self._c(lib().lf_hscene_load_file(self.h, str(path).encode()))
+        return self
+
+    def add_mesh(self, verts, normals):
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 4)
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 4)
+        mid = lib().lf_hscene_add_mesh(self.h, _fp(v), _fp(n), len(v))
+        if mid < 0:
+            raise LFError(1, self.error())
+        return mid
+
+    def add_material(self, m28):
+        m = np.ascontiguousarray(m28, np.float32).reshape(28)
+        return lib().lf_hscene_add_material(self.h, _fp(m))
+
+    def add_instance(self, mesh, xf16, material):
+        x = np.ascontiguousarray(xf16, np.float32).reshape(16)
+        return lib().lf_hscene_add_instance(self.h, mesh, _fp(x), material)
+
+    def add_light(self, l15):
+        l = np.ascontiguousarray(l15, np.float32).reshape(15)
+        return lib().lf_hscene_add_light(self.h, _fp(l))
+
+    def set_camera(self, eye, at, fov_deg, aperture=0.0, focal=1.0):
+        e = np.asarray(eye, np.float32)
+        a = np.asarray(at, np.float32)
+        self._c(lib().lf_hscene_set_camera(self.h, _fp(e), _fp(a), fov_deg, aperture, focal))
+
+    def add_hdr(self, rgb):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        h, w = rgb.shape[:2]
+        self._c(lib().lf_hscene_add_hdr(self.h, _fp(rgb), w, h))
+
+    def build(self, threads=0):
+        self._c(lib().lf_hscene_build(self.h, threads))
+        return self
+
+    def set_instance(self, i, xf16, material):
+        x = np.ascontiguousarray(xf16, np.float32).reshape(16)
+        self._c(lib().lf_hscene_set_instance(self.h, i, _fp(x), material))
+
+    def rebuild_instances(self):
+        self._c(lib().lf_hscene_rebuild_instances(self.h))
+
+    def view(self) -> SceneView:
+        v = SceneView()
+        self._c(lib().lf_hscene_view(self.h, C.byref(v)))
+        return v
+
+    def render_params(self) -> RenderParams:
+        p = RenderParams()
+        self._c(lib().lf_hscene_render_params(self.h, C.byref(p)))
+        return p
+
+    def arrays(self):
+        """Copies of the flat scene arrays (reference layouts) as numpy arrays."""
+        v = self.view()
+
+        def grab(ptr, n, cols, dtype=np.float32):
+            if not ptr or n == 0:
+                return np.zeros((0, cols), dtype)
+            return np.ctypeslib.as_array(ptr, shape=(n * cols,)).astype(dtype, copy=True).reshape(n, cols)
+
+        out = {
+            "nodes": grab(v.nodes, v.num_nodes, 9),
+            "top_level_index": v.top_level_index,
+            "vert_indices": grab(v.vert_indices, v.num_tris, 3, np.int32),
+            "vertices": grab(v.vertices_uvx, v.num_vertices, 4),
+            "normals": grab(v.normals_uvy, v.num_vertices, 4),
+            "materials": grab(v.materials, v.num_materials, 28),
+            "transforms": grab(v.transforms, v.num_instances, 16),
+            "lights": grab(v.lights, v.num_lights, 15),
+        }
+        if v.env_width > 0:
+            out["env_rgb"] = grab(v.env_rgb, v.env_width * v.env_height, 3).reshape(v.env_height, v.env_width, 3)
+            out["env_marginal"] = grab(v.env_marginal, v.env_height, 2)
+            out["env_conditional"] = grab(v.env_conditional, v.env_width * v.env_height, 2)
+        return out
+
+    def layout(self):
+        """(mesh vertex counts, instance mesh ids, instance material ids) before flattening."""
+        cnt = (C.c_int32 * 4)()
+        self._c(lib().lf_hscene_counts(self.h, cnt))
+        mc = np.zeros(cnt[0], np.int32)
+        im = np.zeros(cnt[1], np.int32)
+        imat = np.zeros(cnt[1], np.int32)
+        self._c(lib().lf_hscene_layout(self.h, mc.ctypes.data_as(_I), im.ctypes.data_as(_I), imat.ctypes.data_as(_I)))
+        return mc, im, imat
+
+    # procedural workloads
+    def gen_cornell(self, width=256, height=256):
+        self._c(lib().lf_gen_cornell(self.h, width, height))
+        return self
+
+    def gen_soup(self, instances, tris_per_instance, seed=1):
+        self._c(lib().lf_gen_soup(self.h, instances, tris_per_instance, seed))
+        return self
+
+    def gen_icospheres(self, instances=64, level=6, seed=3, env_w=1024, env_h=512):
+        self._c(lib().lf_gen_icospheres(self.h, instances, level, seed, env_w, env_h))
+        return self
+
+    def gen_room(self, boxes, seed=4):
+        self._c(lib().lf_gen_room(self.h, boxes, seed))
+        return self
+
+
+def gen_rays(lo, hi, n, seed=2, tmax=1.0e6):
+    out = np.empty((n, 8), np.float32)
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    _chk(lib().lf_gen_rays(_fp(lo), _fp(hi), n, seed, tmax, _fp(out)))
+    return out
+
+
+class Context:
+    """One GPU, one stream (lf_ctx)."""
+
+    def __init__(self, device=0):
+        self.h = _P()
+        _chk(lib().lf_ctx_create(device, C.byref(self.h)), lambda: "lf_ctx_create failed (no GPU?)")
+
+    def error(self):
+        return lib().lf_ctx_last_error(self.h).decode()
+
+    def _c(self, st):
+        _chk(st, self.error)
+
+    def close(self):
+        if self.h:
+            lib().lf_ctx_destroy(self.h)
+            self.h = _P()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def sync(self):
+        self._c(lib().lf_ctx_sync(self.h))
+
+    def timer_start(self):
+        self._c(lib().lf_ctx_timer_start(self.h))
+
+    def timer_stop(self):
+        ms = C.c_float()
+        self._c(lib().lf_ctx_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def device_errors(self):
+        return lib().lf_ctx_device_errors(self.h)
+
+    def upload(self, host_scene: HostScene) -> "DeviceScene":
+        v = host_scene.view()
+        return DeviceScene(self, v)
+
+    def trace_closest(self, scene, rays, flags=0):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.empty(len(rays), HIT_DTYPE)
+        self._c(lib().lf_trace_closest(self.h, scene.h, _fp(rays), len(rays), hits.ctypes.data_as(_P), flags))
+        return hits
+
+    def trace_any(self, scene, rays, flags=0):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        occ = np.empty(len(rays), np.uint8)
+        self._c(lib().lf_trace_any(self.h, scene.h, _fp(rays), len(rays), occ.ctypes.data_as(_P), flags))
+        return occ
+
+    def trace_stats(self):
+        out = (C.c_uint64 * 3)()
+        self._c(lib().lf_trace_stats(self.h, out))
+        return list(out)
+
+
+class DeviceScene:
+    def __init__(self, ctx: Context, view: SceneView):
+        self.ctx = ctx
+        self.h = _P()
+        ctx._c(lib().lf_scene_upload(ctx.h, C.byref(view), C.byref(self.h)))
+
+    def set_culling(self, rel, abs_margin=0.0):
+        self.ctx._c(lib().lf_scene_set_culling(self.h, rel, abs_margin))
+
+    def update_instances(self, host_scene: HostScene):
+        v = host_scene.view()
+        self.ctx._c(lib().lf_scene_update_instances(self.h, C.byref(v)))
+
+    def device_bytes(self):
+        return lib().lf_scene_device_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            lib().lf_scene_release(self.h)
+            self.h = _P()
+
+
+class Frame:
+    """Progressive render target (lf_frame)."""
+
+    def __init__(self, ctx: Context, scene: DeviceScene, params: RenderParams, flags=0):
+        self.ctx = ctx
+        self.params = params
+        self.h = _P()
+        ctx._c(lib().lf_frame_create(ctx.h, scene.h, C.byref(params), flags, C.byref(self.h)))
+
+    def render(self, first_sample, count):
+        self.ctx._c(lib().lf_frame_render(self.h, first_sample, count))
+
+    def sync(self):
+        self.ctx._c(lib().lf_frame_sync(self.h))
+
+    def accum(self):
+        out = np.empty((self.params.height, self.params.width, 3), np.float32)
+        self.ctx._c(lib().lf_frame_read_accum(self.h, _fp(out)))
+        return out
+
+    def accum64(self):
+        out = np.empty((self.params.height, self.params.width, 3), np.float64)
+        self.ctx._c(lib().lf_frame_read_accum64(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def paths(self, max_samples):
+        out = np.empty((max_samples, self.params.height, self.params.width, 3), np.float32)
+        self.ctx._c(lib().lf_frame_read_paths(self.h, _fp(out), max_samples))
+        return out
+
+    def reset(self):
+        self.ctx._c(lib().lf_frame_reset(self.h))
+
+    def counters(self):
+        out = (C.c_uint64 * 4)()
+        self.ctx._c(lib().lf_frame_counters(self.h, out))
+        return list(out)
+
+    def set_batch(self, spp):
+        self.ctx._c(lib().lf_frame_set_batch(self.h, spp))
+
+    def close(self):
+        if self.h:
+            lib().lf_frame_release(self.h)
+            self.h = _P()

@@ -1,0 +1,355 @@
+// Device-side scene layout and software BVH traversal (GB300 has no RT cores).
+//
+// Layout in HBM (built from the reference flat arrays by the upload code):
+//  - inner nodes, 64 B each (4 x float4), both children's boxes in one record:
+//      f0 = (Lmin.xyz, Lmax.x) f1 = (Lmax.yz, Rmin.xy) f2 = (Rmin.z, Rmax.xyz)
+//      f3 = (left code, right code, -, -)
+//    A child code >= 0 is an inner-node record; < 0 is a leaf, ~code being
+//    (first packed triangle << 2 | count) on the mesh level and the instance index on the
+//    instance level. One 64 B load replaces the reference's three texel fetches per node
+//    plus two per child box (closest_hit.glsl:102,169-170).
+//  - triangles in packed (leaf) order, 48 B each: v0, e0 = v1 - v0, e1 = v2 - v0
+//    (the reference forms the same differences per test, closest_hit.glsl:119-120).
+//  - instances, 64 B: inverse transform columns 0..3 (xyz) + mesh root code + material;
+//    the reference inverts the 4x4 at every instance-leaf visit (closest_hit.glsl:159-160).
+//  - lights, precomputed plane/normal/scaled edges (closest_hit.glsl:30-35).
+//
+// Traversal keeps the reference's visit order exactly: nearer child first by the value
+// AABBIntersect returns (t0, or t1 when the origin is inside; ties go left), a sentinel
+// separating the instance and mesh levels, strict `t < tBest` acceptance, and the stack
+// capacity of 64 (overflow ends the ray and raises LF_DEVERR_STACK instead of writing past
+// the array). Optional culling skips a child whose entry distance max(t0, 0) exceeds the
+// best hit so far by a safety margin; it never changes which triangle wins except when
+// rounding puts a triangle in front of its own box by more than the margin.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../../include/lavaframe_gb300.h"
+#include "../lf_vec.h"
+
+namespace lfd
+{
+using lfc::v3;
+
+constexpr float kInfinity = 1000000.0f;   // INFINITY in shaders/common/globals.glsl:8
+constexpr float kEps = 0.001f;            // EPS in globals.glsl:9
+constexpr int kStackSize = 64;            // stack[64] in closest_hit.glsl:70
+constexpr int kStackCap = 63;             // one slot of the 64 holds the bottom sentinel
+constexpr int kMaxTraversalSteps = 1 << 22;
+
+// Device error bits (LF_DEVERR_*) are the ones of the C ABI, OR-ed into a status word.
+
+struct DevLight
+{
+    float pos[3], emission[3], u[3], v[3];
+    float radius, area, type;
+    float normal[3];        // normalize(cross(u, v))
+    float planeW;           // dot(normal, pos)
+    float us[3], vs[3];     // u / dot(u,u), v / dot(v,v)
+    float pad[3];
+};
+
+struct DevScene
+{
+    const float4* nodes;        // 4 float4 per inner node
+    const float4* tris;         // 3 float4 per packed triangle
+    const float4* instances;    // 4 float4 per instance
+    const DevLight* lights;
+    int root;                   // instance-level root code
+    int numLights;
+    int numNodes, numTris, numInstances;
+    float cullRel;              // relative culling margin, < 0 disables culling
+    float cullAbs;              // absolute culling margin (a few ulps of the scene extent)
+};
+
+struct TraceStats
+{
+    unsigned long long nodes, tris, leaves;
+};
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// AABBIntersect (intersection.glsl:53-68) returning both the reference's value and the
+// entry distance used for culling.
+__device__ __forceinline__ float box_hit(float bminx, float bminy, float bminz, float bmaxx, float bmaxy,
+                                         float bmaxz, v3 o, v3 invd, float* entry)
+{
+    float fx = (bmaxx - o.x) * invd.x, fy = (bmaxy - o.y) * invd.y, fz = (bmaxz - o.z) * invd.z;
+    float nx = (bminx - o.x) * invd.x, ny = (bminy - o.y) * invd.y, nz = (bminz - o.z) * invd.z;
+    float tmaxx = lfc::fmax_g(fx, nx), tmaxy = lfc::fmax_g(fy, ny), tmaxz = lfc::fmax_g(fz, nz);
+    float tminx = lfc::fmin_g(fx, nx), tminy = lfc::fmin_g(fy, ny), tminz = lfc::fmin_g(fz, nz);
+    float t1 = lfc::fmin_g(tmaxx, lfc::fmin_g(tmaxy, tmaxz));
+    float t0 = lfc::fmax_g(tminx, lfc::fmax_g(tminy, tminz));
+    *entry = t0 > 0.f ? t0 : 0.f;
+    return (t1 >= t0) ? (t0 > 0.f ? t0 : t1) : -1.0f;
+}
+
+// Moller-Trumbore as in closest_hit.glsl:119-134: returns t (= uvt.z) when all of
+// (u, v, t, 1-u-v) are >= 0, else a negative value. u, v returned for barycentrics.
+__device__ __forceinline__ float tri_hit(const float4* tri, v3 o, v3 d, float* pu, float* pv)
+{
+    float4 a = ldg4(tri + 0), b = ldg4(tri + 1), c = ldg4(tri + 2);
+    v3 v0(a.x, a.y, a.z), e0(b.x, b.y, b.z), e1(c.x, c.y, c.z);
+    v3 p = lfc::cross(d, e1);
+    float det = lfc::dot(e0, p);
+    v3 tv = o - v0;
+    v3 q = lfc::cross(tv, e0);
+    float ux = lfc::dot(tv, p) / det;
+    float uy = lfc::dot(d, q) / det;
+    float uz = lfc::dot(e1, q) / det;
+    float uw = 1.0f - ux - uy;
+    *pu = ux;
+    *pv = uy;
+    bool ok = ux >= 0.0f && uy >= 0.0f && uz >= 0.0f && uw >= 0.0f;
+    return ok ? uz : -1.0f;
+}
+
+// Instance inverse transform applied like `vec3(inverse(M) * vec4(x, w))`.
+__device__ __forceinline__ void load_instance(const float4* rec, float m[12], int* root, int* mat)
+{
+    float4 a = ldg4(rec + 0), b = ldg4(rec + 1), c = ldg4(rec + 2), e = ldg4(rec + 3);
+    m[0] = a.x; m[1] = a.y; m[2] = a.z; m[3] = a.w;
+    m[4] = b.x; m[5] = b.y; m[6] = b.z; m[7] = b.w;
+    m[8] = c.x; m[9] = c.y; m[10] = c.z; m[11] = c.w;
+    *root = __float_as_int(e.x);
+    *mat = __float_as_int(e.y);
+}
+
+// columns: c0 = m[0..2], c1 = m[3..5], c2 = m[6..8], c3 = m[9..11]
+__device__ __forceinline__ v3 xform(const float m[12], v3 p, float w)
+{
+    return v3(m[0] * p.x + m[3] * p.y + m[6] * p.z + m[9] * w,
+              m[1] * p.x + m[4] * p.y + m[7] * p.z + m[10] * w,
+              m[2] * p.x + m[5] * p.y + m[8] * p.z + m[11] * w);
+}
+
+struct Hit
+{
+    float t;
+    int inst;      // instance index, -1 if none
+    int prim;      // packed triangle index, -1 if none
+    int light;     // light index when an analytic light is the closest hit, else -1
+};
+
+// RectIntersect / SphereIntersect (intersection.glsl:7-50).
+__device__ __forceinline__ float rect_intersect(const DevLight& L, v3 o, v3 d)
+{
+    v3 n(L.normal[0], L.normal[1], L.normal[2]);
+    float dt = lfc::dot(d, n);
+    float t = (L.planeW - lfc::dot(n, o)) / dt;
+    if (t > kEps)
+    {
+        v3 p = o + d * t;
+        v3 vi = p - v3(L.pos[0], L.pos[1], L.pos[2]);
+        float a1 = lfc::dot(v3(L.us[0], L.us[1], L.us[2]), vi);
+        if (a1 >= 0.f && a1 <= 1.f)
+        {
+            float a2 = lfc::dot(v3(L.vs[0], L.vs[1], L.vs[2]), vi);
+            if (a2 >= 0.f && a2 <= 1.f)
+                return t;
+        }
+    }
+    return kInfinity;
+}
+
+__device__ __forceinline__ float sphere_intersect(const DevLight& L, v3 o, v3 d)
+{
+    v3 op = v3(L.pos[0], L.pos[1], L.pos[2]) - o;
+    float eps = 0.001f;
+    float b = lfc::dot(op, d);
+    float det = b * b - lfc::dot(op, op) + L.radius * L.radius;
+    if (det < 0.f) return kInfinity;
+    det = sqrtf(det);
+    float t1 = b - det;
+    if (t1 > eps) return t1;
+    float t2 = b + det;
+    if (t2 > eps) return t2;
+    return kInfinity;
+}
+
+// Shared two-level traversal. kAny: stop at the first triangle with t < tMax
+// (anyhit.glsl:7-173); otherwise keep the closest (closest_hit.glsl:69-201).
+// Returns device error bits (0 on success).
+template <bool kAny, bool kStats>
+__device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, float* tBest, Hit* out,
+                                             TraceStats* st)
+{
+    int stack[kStackSize];
+    int sp = 0;
+    const int kBlasEnd = (int)0x80000000;
+    const int kEmpty = (int)0x80000001;
+    int code = S.root;
+    bool meshLevel = false;
+    int curInst = -1;
+    v3 ro = o, rd = d;
+    v3 invd = 1.0f / rd;
+    float m[12];
+    uint32_t err = 0;
+    const bool cull = S.cullRel >= 0.f;
+    float t = *tBest;
+    int steps = 0;
+
+    while (true)
+    {
+        if (++steps > kMaxTraversalSteps) { err |= LF_DEVERR_STEPS; break; }
+        if (code == kEmpty)
+        {
+            if (sp == 0) break;
+            code = stack[--sp];
+            if (code == kBlasEnd)
+            {
+                meshLevel = false;
+                ro = o;
+                rd = d;
+                invd = 1.0f / rd;
+                code = kEmpty;
+            }
+            continue;
+        }
+        if (code < 0)
+        {
+            const int payload = ~code;
+            if (meshLevel)
+            {
+                const int first = payload >> 2, cnt = payload & 3;
+                if (kStats) { st->leaves++; st->tris += (unsigned)cnt; }
+                for (int i = 0; i < cnt; ++i)
+                {
+                    float u, v;
+                    float tt = tri_hit(S.tris + (size_t)(first + i) * 3, ro, rd, &u, &v);
+                    if (tt >= 0.f && tt < t)
+                    {
+                        if (kAny)
+                        {
+                            *tBest = tt;
+                            out->inst = curInst;
+                            out->prim = first + i;
+                            return err;
+                        }
+                        t = tt;
+                        out->prim = first + i;
+                        out->inst = curInst;
+                        out->light = -1;
+                    }
+                }
+                code = kEmpty;
+            }
+            else
+            {
+                const int inst = payload;
+                int root, mat;
+                load_instance(S.instances + (size_t)inst * 4, m, &root, &mat);
+                if (sp >= kStackCap) { err |= LF_DEVERR_STACK; break; }
+                stack[sp++] = kBlasEnd;
+                ro = xform(m, o, 1.0f);
+                rd = xform(m, d, 0.0f);
+                invd = 1.0f / rd;
+                meshLevel = true;
+                curInst = inst;
+                code = root;
+            }
+            continue;
+        }
+        const float4* rec = S.nodes + (size_t)code * 4;
+        const float4 f0 = ldg4(rec + 0), f1 = ldg4(rec + 1), f2 = ldg4(rec + 2), f3 = ldg4(rec + 3);
+        if (kStats) st->nodes++;
+        float eL, eR;
+        float hL = box_hit(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, ro, invd, &eL);
+        float hR = box_hit(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, ro, invd, &eR);
+        if (cull)
+        {
+            const float lim = t + t * S.cullRel + S.cullAbs;
+            if (eL > lim) hL = -1.0f;
+            if (eR > lim) hR = -1.0f;
+        }
+        const int cL = __float_as_int(f3.x), cR = __float_as_int(f3.y);
+        if (hL > 0.f && hR > 0.f)
+        {
+            int nearC = cL, farC = cR;
+            if (hL > hR) { nearC = cR; farC = cL; }
+            if (sp >= kStackCap) { err |= LF_DEVERR_STACK; break; }
+            stack[sp++] = farC;
+            code = nearC;
+        }
+        else if (hL > 0.f)
+            code = cL;
+        else if (hR > 0.f)
+            code = cR;
+        else
+            code = kEmpty;
+    }
+    *tBest = t;
+    return err;
+}
+
+// Closest hit: analytic lights first (closest_hit.glsl:13-67), then the BVH.
+template <bool kStats>
+__device__ __forceinline__ uint32_t closest_hit(const DevScene& S, v3 o, v3 d, float tInit, bool useLights,
+                                                Hit* out, TraceStats* st)
+{
+    float t = tInit;
+    out->inst = -1;
+    out->prim = -1;
+    out->light = -1;
+    if (useLights)
+    {
+        for (int i = 0; i < S.numLights; ++i)
+        {
+            const DevLight& L = S.lights[i];
+            float dd;
+            if (L.type == 0.f)
+            {
+                v3 n(L.normal[0], L.normal[1], L.normal[2]);
+                if (lfc::dot(n, d) > 0.f) continue;
+                dd = rect_intersect(L, o, d);
+                if (dd < 0.f) dd = kInfinity;
+                if (dd < t) { t = dd; out->light = i; }
+            }
+            if (L.type == 1.f)
+            {
+                dd = sphere_intersect(L, o, d);
+                if (dd < 0.f) dd = kInfinity;
+                if (dd < t) { t = dd; out->light = i; }
+            }
+        }
+    }
+    uint32_t err = traverse<false, kStats>(S, o, d, &t, out, st);
+    out->t = t;
+    return err;
+}
+
+// Occlusion: lights (two-sided quads, anyhit.glsl:15-50), then the BVH.
+template <bool kStats>
+__device__ __forceinline__ uint32_t any_hit(const DevScene& S, v3 o, v3 d, float maxDist, bool useLights,
+                                            bool* occluded, Hit* out, TraceStats* st)
+{
+    out->inst = -1;
+    out->prim = -1;
+    out->light = -1;
+    *occluded = false;
+    if (useLights)
+    {
+        for (int i = 0; i < S.numLights; ++i)
+        {
+            const DevLight& L = S.lights[i];
+            if (L.type == 0.f)
+            {
+                float dd = rect_intersect(L, o, d);
+                if (dd > 0.f && dd < maxDist) { *occluded = true; out->light = i; out->t = dd; return 0; }
+            }
+            if (L.type == 1.f)
+            {
+                float dd = sphere_intersect(L, o, d);
+                if (dd > 0.f && dd < maxDist) { *occluded = true; out->light = i; out->t = dd; return 0; }
+            }
+        }
+    }
+    float t = maxDist;
+    uint32_t err = traverse<true, kStats>(S, o, d, &t, out, st);
+    *occluded = out->prim >= 0;
+    out->t = *occluded ? t : kInfinity;
+    return err;
+}
+}

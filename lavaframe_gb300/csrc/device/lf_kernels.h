@@ -1,0 +1,54 @@
+// Launch interface of the wavefront kernels and ray queries (implemented in lf_kernels.cu).
+#pragma once
+
+#include "lf_shade.cuh"
+
+namespace lfd
+{
+// Per-path state, structure of arrays, one slot per (sample, pixel) of a batch.
+struct PathSoA
+{
+    float4* o;      // ray origin, w = pdf of the last BSDF sample (MIS at the next hit)
+    float4* d;      // ray direction
+    float4* T;      // throughput
+    float4* L;      // radiance
+    float4* A;      // absorption coefficient
+    uint4* rng;     // PCG4D state
+    int4* info;     // x: pixel index (-1 = off screen), y: depth, z: last material
+    float2* luv;    // texture coordinate of the last triangle hit
+    float4* hit;    // t, instance, packed triangle, light (int bits)
+};
+
+// Next-event rays of one path: up to an environment ray and a light ray plus their
+// unoccluded contributions and the throughput they are weighted by.
+struct ShadowRec
+{
+    float4 a;   // surface position, w: path slot (int bits)
+    float4 b;   // throughput, w: flags (1 env ray, 2 light ray)
+    float4 c;   // environment direction
+    float4 e;   // environment contribution
+    float4 f;   // light direction, w: max distance
+    float4 g;   // light contribution
+};
+
+struct BounceBuffers
+{
+    int* queue[2];
+    int* count;          // [2] queue sizes
+    ShadowRec* shadow;
+    int* shadowCount;
+    uint32_t* status;
+    unsigned long long* ctr;   // [0] paths, [1] extension rays, [2] shadow rays, [3] light clamps
+};
+
+int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,
+                    int* queue, int* qcount, cudaStream_t st);
+int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const BounceBuffers& b, int bounce,
+                  long long cap, cudaStream_t st);
+int launch_accumulate(const Params& P, const PathSoA& ps, int nSamples, float4* accum, double* accum64,
+                      cudaStream_t st);
+int launch_trace_closest(const DevScene& S, const float4* rays, long long n, int4* hits, int lights, bool stats,
+                         uint32_t* status, unsigned long long* stat3, cudaStream_t st);
+int launch_trace_any(const DevScene& S, const float4* rays, long long n, uint8_t* occ, int lights, bool stats,
+                     uint32_t* status, unsigned long long* stat3, cudaStream_t st);
+}

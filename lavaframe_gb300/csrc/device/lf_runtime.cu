@@ -1,0 +1,1040 @@
+// C-ABI runtime: device context, scene upload (re-encoding of the reference flat arrays
+// into the traversal layout described in lf_device.cuh), ray queries and progressive
+// render targets. Host code here must be compiled with -ffp-contract=off: light
+// precomputation and matrix inverses are part of the arithmetic contract.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/lavaframe_gb300.h"
+#include "lf_kernels.h"
+
+using namespace lfd;
+
+struct lf_ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    std::string err;
+    uint32_t* d_status = nullptr;
+    unsigned long long* d_stats = nullptr;   // [3] traversal counters
+    uint32_t devErrors = 0;
+    uint64_t lastStats[3] = {0, 0, 0};
+    // reusable device buffers of the host-pointer ray queries
+    void* scratchRays = nullptr;
+    size_t scratchRaysBytes = 0;
+    void* scratchOut = nullptr;
+    size_t scratchOutBytes = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+struct lf_scene
+{
+    lf_ctx* ctx = nullptr;
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    ShadeScene view{};
+    // re-encoding metadata for instance updates
+    int numRefNodes = 0;
+    int topLevelIndex = 0;
+    int numMeshNodes = 0;       // device records that belong to mesh levels
+    std::vector<int> blasRootCode;   // per reference node index of a mesh root (code), lazily
+    float4* d_nodes = nullptr;
+    size_t nodeCapacity = 0;    // records allocated
+    float4* d_instances = nullptr;
+    ShadeInstance* d_sinst = nullptr;
+    DevMaterial* d_materials = nullptr;
+    int numMaterials = 0;
+    std::vector<int> meshNodeMap;   // reference index -> device record (mesh levels), -1 otherwise
+};
+
+struct lf_frame
+{
+    lf_ctx* ctx = nullptr;
+    lf_scene* scene = nullptr;
+    Params P{};
+    uint32_t flags = 0;
+    int W = 0, H = 0;
+    int numTilesX = 1, numTilesY = 1;
+    int sppBatch = 0;
+    long long cap = 0;   // path slots
+    float4* accum = nullptr;
+    double* accum64 = nullptr;
+    PathSoA ps{};
+    BounceBuffers bb{};
+    std::vector<void*> fixedAllocs;   // accumulation buffers and counters
+    std::vector<void*> allocs;        // path state and queues (sized by the batch)
+    uint64_t paths = 0;
+    int lastBatchSamples = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graphDepth = -1;
+};
+
+namespace
+{
+lf_status fail(lf_ctx* c, lf_status st, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return st;
+}
+
+lf_status cuda_fail(lf_ctx* c, cudaError_t e, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(c, LF_ERR_OOM, m);
+    return fail(c, LF_ERR_CUDA, m);
+}
+
+template <class T>
+cudaError_t dalloc(std::vector<void*>& list, size_t& bytes, T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e == cudaSuccess)
+    {
+        list.push_back(*p);
+        bytes += sizeof(T) * count;
+    }
+    return e;
+}
+
+lf_status check_device(lf_ctx* c)
+{
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronize");
+    uint32_t bits = 0;
+    e = cudaMemcpy(&bits, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
+    if (bits)
+    {
+        c->devErrors |= bits;
+        cudaMemset(c->d_status, 0, sizeof(uint32_t));
+        return fail(c, LF_ERR_DEVICE, "device error bits 0x" + std::to_string(bits));
+    }
+    return LF_OK;
+}
+
+struct RefNode
+{
+    float bmin[3], bmax[3], lr[3];
+};
+
+float ulp_of(float x)
+{
+    x = std::fabs(x);
+    float n = std::nextafter(x, INFINITY);
+    return n - x;
+}
+}
+
+extern "C" {
+
+lf_status lf_ctx_create(int32_t device, lf_ctx** out)
+{
+    if (!out) return LF_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return LF_ERR_CUDA;
+    if (device < 0 || device >= count) return LF_ERR_INVALID;
+    lf_ctx* c = new lf_ctx;
+    c->device = device;
+    if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_status, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_stats, 3 * sizeof(unsigned long long))) != cudaSuccess)
+    {
+        delete c;
+        return e == cudaErrorMemoryAllocation ? LF_ERR_OOM : LF_ERR_CUDA;
+    }
+    cudaMemset(c->d_status, 0, sizeof(uint32_t));
+    cudaMemset(c->d_stats, 0, 3 * sizeof(unsigned long long));
+    *out = c;
+    return LF_OK;
+}
+
+void lf_ctx_destroy(lf_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_status);
+    cudaFree(c->d_stats);
+    cudaFree(c->scratchRays);
+    cudaFree(c->scratchOut);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* lf_ctx_last_error(const lf_ctx* c) { return c ? c->err.c_str() : "null context"; }
+uint32_t lf_ctx_device_errors(const lf_ctx* c) { return c ? c->devErrors : 0; }
+
+lf_status lf_ctx_sync(lf_ctx* c)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    return check_device(c);
+}
+
+lf_status lf_ctx_timer_start(lf_ctx* c)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    for (auto& e : c->ev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) return fail(c, LF_ERR_CUDA, "event create");
+    cudaError_t e = cudaEventRecord(c->ev[0], c->stream);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "event record");
+}
+
+lf_status lf_ctx_timer_stop(lf_ctx* c, float* ms)
+{
+    if (!c || !ms || !c->ev[0]) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaEventRecord(c->ev[1], c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c->ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, c->ev[0], c->ev[1]);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "event timing");
+}
+
+lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out)
+{
+    if (!c || !out) return LF_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaMallocHost");
+}
+
+lf_status lf_host_free(lf_ctx* c, void* p)
+{
+    if (!c) return LF_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaFreeHost(p);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaFreeHost");
+}
+
+lf_status lf_device_alloc(lf_ctx* c, size_t bytes, void** out)
+{
+    if (!c || !out) return LF_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMalloc(out, bytes ? bytes : 1);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaMalloc");
+}
+
+lf_status lf_device_free(lf_ctx* c, void* p)
+{
+    if (!c) return LF_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaFree(p);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaFree");
+}
+
+lf_status lf_copy_to_device(lf_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "copy to device");
+}
+
+lf_status lf_copy_to_host(lf_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "copy to host");
+}
+
+// ------------------------------------------------------------------ scene upload
+namespace
+{
+// Builds the device records for the instance level starting at the reference index
+// `top`, appending to `recs`. Returns the root code.
+lf_status encode_level(lf_ctx* c, const RefNode* nodes, int numNodes, int start, bool meshLevel, int numTris,
+                       int numInstances, std::vector<float4>& recs, std::vector<int>& map, int* rootCode)
+{
+    auto leaf_code = [&](const RefNode& n, int* code) -> bool {
+        int z = (int)n.lr[2];
+        if (meshLevel)
+        {
+            if (z <= 0) return false;
+            int first = (int)n.lr[0], cnt = (int)n.lr[1];
+            if (first < 0 || cnt < 0 || cnt > 3 || first + cnt > numTris) return false;
+            *code = ~((first << 2) | cnt);
+        }
+        else
+        {
+            if (z >= 0) return false;
+            int inst = -z - 1;
+            if (inst >= numInstances) return false;
+            *code = ~inst;
+        }
+        return true;
+    };
+    if (start < 0 || start >= numNodes) return fail(c, LF_ERR_INVALID, "node index out of range");
+    const RefNode& r = nodes[start];
+    if ((int)r.lr[2] != 0)
+    {
+        if (!leaf_code(r, rootCode)) return fail(c, LF_ERR_INVALID, "bad leaf node " + std::to_string(start));
+        return LF_OK;
+    }
+    if (map[start] >= 0)
+    {
+        *rootCode = map[start];
+        return LF_OK;
+    }
+    // iterative pre-order: assign records parent-first
+    struct Item { int ref; };
+    std::vector<int> stack{start};
+    map[start] = (int)(recs.size() / 4);
+    recs.resize(recs.size() + 4);
+    while (!stack.empty())
+    {
+        int ref = stack.back();
+        stack.pop_back();
+        const RefNode& n = nodes[ref];
+        int rec = map[ref];
+        int child[2] = {(int)n.lr[0], (int)n.lr[1]};
+        int code[2];
+        for (int k = 0; k < 2; ++k)
+        {
+            int ci = child[k];
+            if (ci < 0 || ci >= numNodes) return fail(c, LF_ERR_INVALID, "child index out of range at node " + std::to_string(ref));
+            const RefNode& cn = nodes[ci];
+            if ((int)cn.lr[2] != 0)
+            {
+                if (!leaf_code(cn, &code[k])) return fail(c, LF_ERR_INVALID, "bad leaf node " + std::to_string(ci));
+            }
+            else
+            {
+                if (map[ci] >= 0) return fail(c, LF_ERR_INVALID, "node referenced twice: " + std::to_string(ci));
+                map[ci] = (int)(recs.size() / 4);
+                recs.resize(recs.size() + 4);
+                code[k] = map[ci];
+            }
+        }
+        const RefNode& L = nodes[child[0]];
+        const RefNode& R = nodes[child[1]];
+        float4* o = &recs[(size_t)rec * 4];
+        o[0] = make_float4(L.bmin[0], L.bmin[1], L.bmin[2], L.bmax[0]);
+        o[1] = make_float4(L.bmax[1], L.bmax[2], R.bmin[0], R.bmin[1]);
+        o[2] = make_float4(R.bmin[2], R.bmax[0], R.bmax[1], R.bmax[2]);
+        float cf0, cf1;
+        std::memcpy(&cf0, &code[0], 4);
+        std::memcpy(&cf1, &code[1], 4);
+        o[3] = make_float4(cf0, cf1, 0.f, 0.f);
+        // push right then left so the left subtree is laid out first
+        if ((int)R.lr[2] == 0) stack.push_back(child[1]);
+        if ((int)L.lr[2] == 0) stack.push_back(child[0]);
+    }
+    *rootCode = map[start];
+    return LF_OK;
+}
+
+void make_light(const float* l15, DevLight& d)
+{
+    using lfc::v3;
+    std::memset(&d, 0, sizeof d);
+    for (int k = 0; k < 3; ++k)
+    {
+        d.pos[k] = l15[k];
+        d.emission[k] = l15[3 + k];
+        d.u[k] = l15[6 + k];
+        d.v[k] = l15[9 + k];
+    }
+    d.radius = l15[12];
+    d.area = l15[13];
+    d.type = l15[14];
+    v3 u(d.u[0], d.u[1], d.u[2]), v(d.v[0], d.v[1], d.v[2]), p(d.pos[0], d.pos[1], d.pos[2]);
+    v3 n = lfc::normalize(lfc::cross(u, v));
+    d.normal[0] = n.x; d.normal[1] = n.y; d.normal[2] = n.z;
+    d.planeW = lfc::dot(n, p);
+    v3 us = u * (1.0f / lfc::dot(u, u));
+    v3 vs = v * (1.0f / lfc::dot(v, v));
+    d.us[0] = us.x; d.us[1] = us.y; d.us[2] = us.z;
+    d.vs[0] = vs.x; d.vs[1] = vs.y; d.vs[2] = vs.z;
+}
+
+lf_status encode_instances(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, std::vector<float4>& recs,
+                           std::vector<int>& map, std::vector<float4>& inst, std::vector<ShadeInstance>& sinst,
+                           int* tlasRoot)
+{
+    const int ni = v->num_instances;
+    // instance level
+    lf_status st = encode_level(c, nodes, v->num_nodes, v->top_level_index, false, v->num_tris, ni, recs, map, tlasRoot);
+    if (st != LF_OK) return st;
+    // instance records from the instance-level leaves
+    std::vector<int> instRootRef(ni, -1), instMat(ni, -1);
+    std::vector<int> stack{v->top_level_index};
+    while (!stack.empty())
+    {
+        int ref = stack.back();
+        stack.pop_back();
+        const RefNode& n = nodes[ref];
+        int z = (int)n.lr[2];
+        if (z < 0)
+        {
+            int i = -z - 1;
+            if (instRootRef[i] != -1) return fail(c, LF_ERR_INVALID, "instance listed twice in the instance tree");
+            instRootRef[i] = (int)n.lr[0];
+            instMat[i] = (int)n.lr[1];
+        }
+        else if (z == 0)
+        {
+            stack.push_back((int)n.lr[1]);
+            stack.push_back((int)n.lr[0]);
+        }
+        else
+            return fail(c, LF_ERR_INVALID, "mesh leaf inside the instance tree");
+    }
+    inst.assign((size_t)ni * 4, make_float4(0, 0, 0, 0));
+    sinst.assign(ni, ShadeInstance{});
+    for (int i = 0; i < ni; ++i)
+    {
+        const float* M = v->transforms + (size_t)i * 16;
+        float inv[16];
+        lfc::inverse4(M, inv);
+        int rootCode = ~0;   // empty leaf for instances that no leaf references
+        if (instRootRef[i] >= 0)
+        {
+            st = encode_level(c, nodes, v->num_nodes, instRootRef[i], true, v->num_tris, ni, recs, map, &rootCode);
+            if (st != LF_OK) return st;
+            if (instMat[i] < 0 || instMat[i] >= v->num_materials)
+                return fail(c, LF_ERR_INVALID, "instance material out of range");
+        }
+        float rc, mc;
+        int mat = instMat[i] < 0 ? 0 : instMat[i];
+        std::memcpy(&rc, &rootCode, 4);
+        std::memcpy(&mc, &mat, 4);
+        float4* o = &inst[(size_t)i * 4];
+        // columns c0..c3 (xyz) of the inverse
+        o[0] = make_float4(inv[0], inv[1], inv[2], inv[4]);
+        o[1] = make_float4(inv[5], inv[6], inv[8], inv[9]);
+        o[2] = make_float4(inv[10], inv[12], inv[13], inv[14]);
+        o[3] = make_float4(rc, mc, 0.f, 0.f);
+        ShadeInstance& s = sinst[i];
+        for (int col = 0; col < 4; ++col)
+            for (int r = 0; r < 3; ++r) s.fwd[col * 3 + r] = M[col * 4 + r];
+        lfc::normal_matrix(M, s.nrm);
+        s.material = mat;
+    }
+    return LF_OK;
+}
+}
+
+lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
+{
+    if (!c || !v || !out) return LF_ERR_INVALID;
+    *out = nullptr;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    if (v->num_nodes <= 0 || !v->nodes || v->num_tris <= 0 || !v->vert_indices || v->num_vertices <= 0 ||
+        !v->vertices_uvx || !v->normals_uvy || v->num_materials <= 0 || !v->materials || v->num_instances <= 0 ||
+        !v->transforms || v->top_level_index < 0 || v->top_level_index >= v->num_nodes ||
+        (v->num_lights > 0 && !v->lights))
+        return fail(c, LF_ERR_INVALID, "incomplete scene view");
+    const RefNode* nodes = reinterpret_cast<const RefNode*>(v->nodes);
+
+    std::vector<float4> recs;
+    recs.reserve((size_t)v->num_nodes * 4);
+    std::vector<int> map(v->num_nodes, -1);
+    std::vector<float4> inst;
+    std::vector<ShadeInstance> sinst;
+    int tlasRoot = 0;
+    lf_status st = encode_instances(c, v, nodes, recs, map, inst, sinst, &tlasRoot);
+    if (st != LF_OK) return st;
+
+    // triangles in packed order: v0, v1 - v0, v2 - v0
+    std::vector<float4> tris((size_t)v->num_tris * 3);
+    std::vector<int4> vidx(v->num_tris);
+    float extent = 0.f;
+    for (int k = 0; k < v->num_tris; ++k)
+    {
+        const int* ix = v->vert_indices + (size_t)k * 3;
+        for (int j = 0; j < 3; ++j)
+            if (ix[j] < 0 || ix[j] >= v->num_vertices) return fail(c, LF_ERR_INVALID, "vertex index out of range");
+        const float* a = v->vertices_uvx + (size_t)ix[0] * 4;
+        const float* b = v->vertices_uvx + (size_t)ix[1] * 4;
+        const float* cc = v->vertices_uvx + (size_t)ix[2] * 4;
+        tris[(size_t)k * 3 + 0] = make_float4(a[0], a[1], a[2], 0.f);
+        tris[(size_t)k * 3 + 1] = make_float4(b[0] - a[0], b[1] - a[1], b[2] - a[2], 0.f);
+        tris[(size_t)k * 3 + 2] = make_float4(cc[0] - a[0], cc[1] - a[1], cc[2] - a[2], 0.f);
+        vidx[k] = make_int4(ix[0], ix[1], ix[2], 0);
+    }
+    for (int i = 0; i < v->num_nodes; ++i)
+        for (int k = 0; k < 3; ++k)
+        {
+            float m = std::max(std::fabs(nodes[i].bmin[k]), std::fabs(nodes[i].bmax[k]));
+            if (m < 3.0e38f) extent = std::max(extent, m);
+        }
+
+    std::vector<DevLight> lights(std::max(v->num_lights, 0));
+    for (int i = 0; i < v->num_lights; ++i) make_light(v->lights + (size_t)i * 15, lights[i]);
+
+    lf_scene* sc = new lf_scene;
+    sc->ctx = c;
+    cudaError_t e = cudaSuccess;
+    float4 *d_nodes, *d_tris, *d_inst, *d_verts, *d_norms;
+    DevLight* d_lights;
+    int4* d_vidx;
+    DevMaterial* d_mats;
+    ShadeInstance* d_sinst;
+    auto A = [&](auto** p, size_t n) {
+        if (e == cudaSuccess) e = dalloc(sc->allocs, sc->bytes, p, n);
+    };
+    A(&d_nodes, recs.size());
+    A(&d_tris, tris.size());
+    A(&d_inst, inst.size());
+    A(&d_lights, lights.size());
+    A(&d_vidx, vidx.size());
+    A(&d_verts, (size_t)v->num_vertices);
+    A(&d_norms, (size_t)v->num_vertices);
+    A(&d_mats, (size_t)v->num_materials);
+    A(&d_sinst, sinst.size());
+    float* d_env = nullptr;
+    float2 *d_marg = nullptr, *d_cond = nullptr;
+    uint8_t* d_tex = nullptr;
+    bool hasEnv = v->env_rgb && v->env_width > 0 && v->env_height > 0 && v->env_marginal && v->env_conditional;
+    if (hasEnv)
+    {
+        A(&d_env, (size_t)v->env_width * v->env_height * 3);
+        A(&d_marg, (size_t)v->env_height);
+        A(&d_cond, (size_t)v->env_width * v->env_height);
+    }
+    bool hasTex = v->textures && v->num_textures > 0 && v->tex_width > 0 && v->tex_height > 0;
+    if (hasTex) A(&d_tex, (size_t)v->num_textures * v->tex_width * v->tex_height * 4);
+    if (e != cudaSuccess)
+    {
+        lf_scene_release(sc);
+        return cuda_fail(c, e, "scene allocation");
+    }
+    auto H2D = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    H2D(d_nodes, recs.data(), recs.size() * sizeof(float4));
+    H2D(d_tris, tris.data(), tris.size() * sizeof(float4));
+    H2D(d_inst, inst.data(), inst.size() * sizeof(float4));
+    H2D(d_lights, lights.data(), lights.size() * sizeof(DevLight));
+    H2D(d_vidx, vidx.data(), vidx.size() * sizeof(int4));
+    H2D(d_verts, v->vertices_uvx, (size_t)v->num_vertices * 16);
+    H2D(d_norms, v->normals_uvy, (size_t)v->num_vertices * 16);
+    H2D(d_mats, v->materials, (size_t)v->num_materials * sizeof(DevMaterial));
+    H2D(d_sinst, sinst.data(), sinst.size() * sizeof(ShadeInstance));
+    if (hasEnv)
+    {
+        H2D(d_env, v->env_rgb, (size_t)v->env_width * v->env_height * 3 * sizeof(float));
+        H2D(d_marg, v->env_marginal, (size_t)v->env_height * sizeof(float2));
+        H2D(d_cond, v->env_conditional, (size_t)v->env_width * v->env_height * sizeof(float2));
+    }
+    if (hasTex) H2D(d_tex, v->textures, (size_t)v->num_textures * v->tex_width * v->tex_height * 4);
+    if (e != cudaSuccess)
+    {
+        lf_scene_release(sc);
+        return cuda_fail(c, e, "scene upload");
+    }
+
+    ShadeScene& S = sc->view;
+    S.trav.nodes = d_nodes;
+    S.trav.tris = d_tris;
+    S.trav.instances = d_inst;
+    S.trav.lights = d_lights;
+    S.trav.root = tlasRoot;
+    S.trav.numLights = v->num_lights;
+    S.trav.numNodes = (int)(recs.size() / 4);
+    S.trav.numTris = v->num_tris;
+    S.trav.numInstances = v->num_instances;
+    S.trav.cullRel = 1.0e-4f;
+    S.trav.cullAbs = 64.0f * ulp_of(extent);
+    S.vertIndices = d_vidx;
+    S.vertices = d_verts;
+    S.normals = d_norms;
+    S.materials = d_mats;
+    S.inst = d_sinst;
+    S.numMaterials = v->num_materials;
+    if (hasEnv)
+    {
+        S.env.rgb = d_env;
+        S.env.marginal = d_marg;
+        S.env.cond = d_cond;
+        S.env.w = v->env_width;
+        S.env.h = v->env_height;
+        S.env.resolution = (float)(v->env_width * v->env_height);
+    }
+    S.env.multiplier = 1.0f;
+    if (hasTex)
+    {
+        S.tex.rgba = d_tex;
+        S.tex.w = v->tex_width;
+        S.tex.h = v->tex_height;
+        S.tex.layers = v->num_textures;
+    }
+    sc->numRefNodes = v->num_nodes;
+    sc->topLevelIndex = v->top_level_index;
+    sc->d_nodes = d_nodes;
+    sc->nodeCapacity = recs.size() / 4;
+    sc->d_instances = d_inst;
+    sc->d_sinst = d_sinst;
+    sc->d_materials = d_mats;
+    sc->numMaterials = v->num_materials;
+    *out = sc;
+    return LF_OK;
+}
+
+lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
+{
+    if (!sc || !v) return LF_ERR_INVALID;
+    lf_ctx* c = sc->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    if (v->num_nodes != sc->numRefNodes || v->top_level_index != sc->topLevelIndex ||
+        v->num_instances != sc->view.trav.numInstances || v->num_materials != sc->numMaterials)
+        return fail(c, LF_ERR_INVALID, "instance update must keep node, instance and material counts");
+    // Re-encode everything host-side (mesh levels are unchanged, so the record count is
+    // identical) and overwrite the node, instance and material arrays in place.
+    const RefNode* nodes = reinterpret_cast<const RefNode*>(v->nodes);
+    std::vector<float4> recs;
+    recs.reserve(sc->nodeCapacity * 4);
+    std::vector<int> map(v->num_nodes, -1);
+    std::vector<float4> inst;
+    std::vector<ShadeInstance> sinst;
+    int tlasRoot = 0;
+    lf_status st = encode_instances(c, v, nodes, recs, map, inst, sinst, &tlasRoot);
+    if (st != LF_OK) return st;
+    if (recs.size() / 4 > sc->nodeCapacity) return fail(c, LF_ERR_INVALID, "instance update grew the node array");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(sc->d_nodes, recs.data(), recs.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(sc->d_instances, inst.data(), inst.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(sc->d_sinst, sinst.data(), sinst.size() * sizeof(ShadeInstance), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(sc->d_materials, v->materials, (size_t)v->num_materials * sizeof(DevMaterial), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "instance update");
+    sc->view.trav.root = tlasRoot;
+    sc->view.trav.numNodes = (int)(recs.size() / 4);
+    return LF_OK;
+}
+
+lf_status lf_scene_release(lf_scene* sc)
+{
+    if (!sc) return LF_ERR_INVALID;
+    if (sc->ctx)
+    {
+        cudaSetDevice(sc->ctx->device);
+        cudaStreamSynchronize(sc->ctx->stream);
+    }
+    for (void* p : sc->allocs) cudaFree(p);
+    delete sc;
+    return LF_OK;
+}
+
+lf_status lf_scene_set_culling(lf_scene* sc, float rel, float abs_margin)
+{
+    if (!sc) return LF_ERR_INVALID;
+    sc->view.trav.cullRel = rel;
+    sc->view.trav.cullAbs = abs_margin;
+    return LF_OK;
+}
+
+size_t lf_scene_device_bytes(const lf_scene* sc) { return sc ? sc->bytes : 0; }
+
+// ------------------------------------------------------------------ ray queries
+lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_hits, uint32_t flags)
+{
+    if (!c || !sc || (n > 0 && (!d_rays || !d_hits)) || n < 0) return LF_ERR_INVALID;
+    if (n == 0) return LF_OK;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    bool stats = (flags & LF_TRACE_STATS) != 0;
+    if (stats) cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream);
+    int e = launch_trace_closest(sc->view.trav, (const float4*)d_rays, n, (int4*)d_hits, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+                                 stats, c->d_status, c->d_stats, c->stream);
+    if (e) return cuda_fail(c, (cudaError_t)e, "trace launch");
+    return LF_OK;
+}
+
+lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_occ, uint32_t flags)
+{
+    if (!c || !sc || (n > 0 && (!d_rays || !d_occ)) || n < 0) return LF_ERR_INVALID;
+    if (n == 0) return LF_OK;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    bool stats = (flags & LF_TRACE_STATS) != 0;
+    if (stats) cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream);
+    int e = launch_trace_any(sc->view.trav, (const float4*)d_rays, n, (uint8_t*)d_occ, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+                             stats, c->d_status, c->d_stats, c->stream);
+    if (e) return cuda_fail(c, (cudaError_t)e, "trace launch");
+    return LF_OK;
+}
+
+}   // extern "C"
+
+namespace
+{
+template <class Launch>
+lf_status trace_host(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, void* out, size_t outElem, uint32_t flags,
+                     Launch launch)
+{
+    if (!c || !sc || n < 0 || (n > 0 && (!rays || !out))) return LF_ERR_INVALID;
+    if (n == 0) return LF_OK;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    auto ensure = [&](void** buf, size_t* cap, size_t bytes) -> cudaError_t {
+        if (*cap >= bytes) return cudaSuccess;
+        cudaStreamSynchronize(c->stream);
+        cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
+        cudaError_t err = cudaMalloc(buf, bytes);
+        if (err == cudaSuccess) *cap = bytes;
+        return err;
+    };
+    cudaError_t e = ensure(&c->scratchRays, &c->scratchRaysBytes, (size_t)n * 32);
+    if (e == cudaSuccess) e = ensure(&c->scratchOut, &c->scratchOutBytes, (size_t)n * outElem);
+    void* d_rays = c->scratchRays;
+    void* d_out = c->scratchOut;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
+    lf_status st = LF_OK;
+    if (e == cudaSuccess) st = launch(d_rays, d_out);
+    if (e == cudaSuccess && st == LF_OK) e = cudaMemcpyAsync(out, d_out, (size_t)n * outElem, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && st == LF_OK) st = check_device(c);
+    if (e == cudaSuccess && st == LF_OK && (flags & LF_TRACE_STATS))
+    {
+        unsigned long long s[3];
+        cudaMemcpy(s, c->d_stats, sizeof s, cudaMemcpyDeviceToHost);
+        for (int k = 0; k < 3; ++k) c->lastStats[k] = s[k];
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "trace");
+    return st;
+}
+}
+
+extern "C" {
+
+lf_status lf_trace_closest(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, lf_hit* hits, uint32_t flags)
+{
+    return trace_host(c, sc, rays, n, hits, sizeof(lf_hit), flags, [&](void* dr, void* dout) {
+        return lf_trace_closest_device(c, sc, dr, n, dout, flags);
+    });
+}
+
+lf_status lf_trace_any(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, uint8_t* occ, uint32_t flags)
+{
+    return trace_host(c, sc, rays, n, occ, 1, flags, [&](void* dr, void* dout) {
+        return lf_trace_any_device(c, sc, dr, n, dout, flags);
+    });
+}
+
+lf_status lf_trace_stats(const lf_ctx* c, uint64_t out3[3])
+{
+    if (!c || !out3) return LF_ERR_INVALID;
+    for (int k = 0; k < 3; ++k) out3[k] = c->lastStats[k];
+    return LF_OK;
+}
+
+// ------------------------------------------------------------------ frames
+namespace
+{
+void fill_params(Params& P, const lf_render_params* p, const lf_scene* sc)
+{
+    std::memset(&P, 0, sizeof P);
+    P.width = p->width;
+    P.height = p->height;
+    P.tileW = p->tile_width > 0 ? p->tile_width : p->width;
+    P.tileH = p->tile_height > 0 ? p->tile_height : p->height;
+    // TiledRenderer.cpp:232-233: 1 / (screen / tile), in float
+    P.invNumTilesX = 1.0f / ((float)p->width / (float)P.tileW);
+    P.invNumTilesY = 1.0f / ((float)p->height / (float)P.tileH);
+    P.maxDepth = p->max_depth;
+    P.rrEnabled = p->enable_rr;
+    P.rrDepth = p->rr_depth;
+    bool envData = sc->view.env.rgb != nullptr;
+    P.constantBg = p->use_constant_bg;
+    P.envOnMiss = (p->use_env_map && envData) ? 1 : 0;
+    P.useEnv = (P.envOnMiss && !P.constantBg) ? 1 : 0;
+    P.useLights = sc->view.trav.numLights > 0 ? 1 : 0;
+    for (int k = 0; k < 3; ++k)
+    {
+        P.bg[k] = p->bg_color[k];
+        P.cam_pos[k] = p->cam_position[k];
+        P.cam_right[k] = p->cam_right[k];
+        P.cam_up[k] = p->cam_up[k];
+        P.cam_fwd[k] = p->cam_forward[k];
+    }
+    P.fov = p->cam_fov;
+    P.focalDist = p->cam_focal_dist;
+    P.aperture = p->cam_aperture;
+    P.seed = p->seed;
+    P.frameBase = p->frame_base;
+    P.frameStride = 1;
+    P.tileOrdinal = 0;
+    P.hdrMultiplier = p->hdr_multiplier;
+}
+
+void free_frame_buffers(lf_frame* f)
+{
+    for (void* q : f->allocs) cudaFree(q);
+    f->allocs.clear();
+    f->cap = 0;
+}
+
+lf_status alloc_paths(lf_frame* f, long long cap)
+{
+    lf_ctx* c = f->ctx;
+    size_t bytes = 0;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto** p, size_t n) {
+        if (e == cudaSuccess) e = dalloc(f->allocs, bytes, p, n);
+    };
+    A(&f->ps.o, cap);
+    A(&f->ps.d, cap);
+    A(&f->ps.T, cap);
+    A(&f->ps.L, cap);
+    A(&f->ps.A, cap);
+    A(&f->ps.rng, cap);
+    A(&f->ps.info, cap);
+    A(&f->ps.luv, cap);
+    A(&f->ps.hit, cap);
+    A(&f->bb.queue[0], cap);
+    A(&f->bb.queue[1], cap);
+    A(&f->bb.count, 2);
+    A(&f->bb.shadow, cap);
+    A(&f->bb.shadowCount, 1);
+    if (e != cudaSuccess)
+    {
+        free_frame_buffers(f);
+        return cuda_fail(c, e, "path state allocation");
+    }
+    f->cap = cap;
+    return LF_OK;
+}
+}
+
+lf_status lf_frame_create(lf_ctx* c, lf_scene* sc, const lf_render_params* p, uint32_t flags, lf_frame** out)
+{
+    if (!c || !sc || !p || !out) return LF_ERR_INVALID;
+    *out = nullptr;
+    if (p->width <= 0 || p->height <= 0 || p->max_depth < 0 || p->tile_width < 0 || p->tile_height < 0)
+        return fail(c, LF_ERR_INVALID, "bad render parameters");
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    lf_frame* f = new lf_frame;
+    f->ctx = c;
+    f->scene = sc;
+    f->flags = flags;
+    f->W = p->width;
+    f->H = p->height;
+    fill_params(f->P, p, sc);
+    f->numTilesX = (f->W + f->P.tileW - 1) / f->P.tileW;
+    f->numTilesY = (f->H + f->P.tileH - 1) / f->P.tileH;
+    // default batch: about 8M path slots
+    long long tilePix = (long long)f->P.tileW * f->P.tileH;
+    f->sppBatch = (int)std::max(1LL, std::min(64LL, (8LL << 20) / tilePix));
+    size_t bytes = 0;
+    unsigned long long* ctr = nullptr;
+    cudaError_t e = dalloc(f->fixedAllocs, bytes, &f->accum, (size_t)f->W * f->H);
+    if (e == cudaSuccess && (flags & LF_FRAME_FP64_ACCUM)) e = dalloc(f->fixedAllocs, bytes, &f->accum64, (size_t)f->W * f->H * 3);
+    if (e == cudaSuccess) e = dalloc(f->fixedAllocs, bytes, &ctr, 4);
+    f->bb.ctr = ctr;
+    f->bb.status = c->d_status;
+    lf_status st = e == cudaSuccess ? alloc_paths(f, (long long)f->sppBatch * tilePix) : cuda_fail(c, e, "frame allocation");
+    if (st != LF_OK)
+    {
+        for (void* q : f->fixedAllocs) cudaFree(q);
+        delete f;
+        return st;
+    }
+    cudaMemsetAsync(f->accum, 0, sizeof(float4) * (size_t)f->W * f->H, c->stream);
+    if (f->accum64) cudaMemsetAsync(f->accum64, 0, sizeof(double) * (size_t)f->W * f->H * 3, c->stream);
+    cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), c->stream);
+    *out = f;
+    return LF_OK;
+}
+
+lf_status lf_frame_set_batch(lf_frame* f, int32_t spb)
+{
+    if (!f || spb < 0) return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    long long tilePix = (long long)f->P.tileW * f->P.tileH;
+    int want = spb == 0 ? (int)std::max(1LL, std::min(64LL, (8LL << 20) / tilePix)) : spb;
+    if (want == f->sppBatch) return LF_OK;
+    cudaStreamSynchronize(c->stream);
+    free_frame_buffers(f);
+    if (f->graph)
+    {
+        cudaGraphExecDestroy(f->graph);
+        f->graph = nullptr;
+    }
+    f->sppBatch = want;
+    lf_status st = alloc_paths(f, (long long)want * tilePix);
+    return st;
+}
+
+namespace
+{
+// One batch of samples on one tile: generate, maxDepth bounces, accumulate.
+lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
+{
+    lf_ctx* c = f->ctx;
+    const ShadeScene& S = f->scene->view;
+    ShadeScene Sv = S;
+    Sv.env.multiplier = P.hdrMultiplier;
+    long long tilePix = (long long)P.tileW * P.tileH;
+    long long cap = (long long)n * tilePix;
+    cudaMemsetAsync(f->bb.count, 0, 2 * sizeof(int), c->stream);
+    int e = launch_generate(Sv, P, f->ps, firstSample, n, f->bb.queue[0], f->bb.count, c->stream);
+    if (e) return cuda_fail(c, (cudaError_t)e, "generate launch");
+    for (int b = 0; b < P.maxDepth; ++b)
+    {
+        e = launch_bounce(Sv, P, f->ps, f->bb, b, cap, c->stream);
+        if (e) return cuda_fail(c, (cudaError_t)e, "bounce launch");
+    }
+    e = launch_accumulate(P, f->ps, n, f->accum, f->accum64, c->stream);
+    if (e) return cuda_fail(c, (cudaError_t)e, "accumulate launch");
+    f->lastBatchSamples = n;
+    return LF_OK;
+}
+}
+
+lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count)
+{
+    if (!f || count < 0 || first_sample < 0) return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    Params P = f->P;
+    const bool tiledFrames = (f->flags & LF_FRAME_TILED_FRAMES) != 0;
+    P.frameStride = tiledFrames ? f->numTilesX * f->numTilesY : 1;
+    int s = 0;
+    while (s < count)
+    {
+        int n = std::min(f->sppBatch, count - s);
+        for (int ty = f->numTilesY - 1; ty >= 0; --ty)      // TiledRenderer order: top tile row first
+            for (int tx = 0; tx < f->numTilesX; ++tx)
+            {
+                P.tileX = tx;
+                P.tileY = ty;
+                P.tileOrdinal = tiledFrames ? (f->numTilesY - 1 - ty) * f->numTilesX + tx : 0;
+                lf_status st = run_batch(f, P, first_sample + s, n);
+                if (st != LF_OK) return st;
+            }
+        s += n;
+    }
+    f->paths += (uint64_t)count * f->W * f->H;
+    return LF_OK;
+}
+
+lf_status lf_frame_sync(lf_frame* f)
+{
+    if (!f) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(f->ctx->mu);
+    cudaSetDevice(f->ctx->device);
+    return check_device(f->ctx);
+}
+
+lf_status lf_frame_read_accum(lf_frame* f, float* rgb)
+{
+    if (!f || !rgb) return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    std::vector<float4> tmp((size_t)f->W * f->H);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), f->accum, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "accum readback");
+    for (size_t i = 0; i < tmp.size(); ++i)
+    {
+        rgb[i * 3 + 0] = tmp[i].x;
+        rgb[i * 3 + 1] = tmp[i].y;
+        rgb[i * 3 + 2] = tmp[i].z;
+    }
+    return check_device(c);
+}
+
+lf_status lf_frame_read_accum64(lf_frame* f, double* rgb)
+{
+    if (!f || !rgb) return LF_ERR_INVALID;
+    if (!f->accum64) return fail(f->ctx, LF_ERR_STATE, "frame was created without LF_FRAME_FP64_ACCUM");
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMemcpyAsync(rgb, f->accum64, sizeof(double) * (size_t)f->W * f->H * 3, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "accum64 readback");
+    return check_device(c);
+}
+
+lf_status lf_frame_read_paths(lf_frame* f, float* rgb, int32_t max_samples)
+{
+    if (!f || !rgb || max_samples <= 0) return LF_ERR_INVALID;
+    if (f->numTilesX * f->numTilesY != 1) return fail(f->ctx, LF_ERR_STATE, "path readback needs a single tile");
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    int n = std::min(max_samples, f->lastBatchSamples);
+    size_t pix = (size_t)f->W * f->H;
+    std::vector<float4> tmp(pix * n);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), f->ps.L, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "path readback");
+    for (size_t i = 0; i < tmp.size(); ++i)
+    {
+        rgb[i * 3 + 0] = tmp[i].x;
+        rgb[i * 3 + 1] = tmp[i].y;
+        rgb[i * 3 + 2] = tmp[i].z;
+    }
+    return check_device(c);
+}
+
+lf_status lf_frame_reset(lf_frame* f)
+{
+    if (!f) return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaMemsetAsync(f->accum, 0, sizeof(float4) * (size_t)f->W * f->H, c->stream);
+    if (f->accum64) cudaMemsetAsync(f->accum64, 0, sizeof(double) * (size_t)f->W * f->H * 3, c->stream);
+    cudaMemsetAsync(f->bb.ctr, 0, 4 * sizeof(unsigned long long), c->stream);
+    f->paths = 0;
+    return LF_OK;
+}
+
+lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4])
+{
+    if (!f || !out4) return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    unsigned long long v[4];
+    cudaError_t e = cudaMemcpyAsync(v, f->bb.ctr, sizeof v, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "counter readback");
+    for (int k = 0; k < 4; ++k) out4[k] = v[k];
+    out4[0] = f->paths;
+    return LF_OK;
+}
+
+lf_status lf_frame_release(lf_frame* f)
+{
+    if (!f) return LF_ERR_INVALID;
+    cudaSetDevice(f->ctx->device);
+    cudaStreamSynchronize(f->ctx->stream);
+    if (f->graph) cudaGraphExecDestroy(f->graph);
+    for (void* q : f->allocs) cudaFree(q);
+    for (void* q : f->fixedAllocs) cudaFree(q);
+    delete f;
+    return LF_OK;
+}
+}

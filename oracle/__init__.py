@@ -1,0 +1,89 @@
+"""CPU oracle (test infrastructure): ctypes wrapper of oracle/liblfo.so.
+
+The oracle restates the reference GLSL path tracer in scalar C++ and runs it on the host
+cores. Only tests, the smoke check and the bench's CPU-baseline leg use it, as the checker;
+the product path never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liblfo.so"
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise RuntimeError(f"{LIB} missing; build with lavaframe_gb300.build.build_oracle()")
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        L.lfo_trace_closest.argtypes = [P, P, C.c_int64, P, C.c_int32, C.c_float, C.c_float, C.c_int32, P]
+        L.lfo_trace_any.argtypes = [P, P, C.c_int64, P, C.c_int32, C.c_float, C.c_float, C.c_int32, P]
+        L.lfo_render.argtypes = [P, P, C.c_int32, C.c_int32, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                 C.c_float, P]
+        L.lfo_math.argtypes = [C.c_int32, P, P, C.c_int64, P]
+        L.lfo_rand_sequence.argtypes = [C.c_float, C.c_float, C.c_int32, C.c_uint32, C.c_int32, P]
+        _lib = L
+    return _lib
+
+
+MATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan2": 3, "acos": 4, "exp": 5, "log": 6, "pow": 7}
+
+
+def contract(fn, x, y=None):
+    """Evaluates a function of the arithmetic contract on the host, element-wise."""
+    x = np.ascontiguousarray(x, np.float32)
+    yy = None if y is None else np.ascontiguousarray(y, np.float32)
+    out = np.empty_like(x)
+    lib().lfo_math(MATH_FN[fn], x.ctypes.data, None if yy is None else yy.ctypes.data, x.size, out.ctypes.data)
+    return out
+
+
+def rand_sequence(px, py, frame, n, seed=0):
+    out = np.empty(n, np.float32)
+    lib().lfo_rand_sequence(px, py, frame, seed, n, out.ctypes.data)
+    return out
+
+
+HIT_DTYPE = np.dtype([("t", "<f4"), ("instance", "<i4"), ("prim", "<i4"), ("light", "<i4")])
+
+
+def trace_closest(view, rays, lights=False, cull_rel=-1.0, cull_abs=0.0, threads=0):
+    """Hits (t, instance, packed triangle, light) per ray; cull_rel < 0 = shader semantics."""
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    hits = np.empty(len(rays), HIT_DTYPE)
+    stats = np.zeros(5, np.uint64)
+    lib().lfo_trace_closest(C.addressof(view), rays.ctypes.data, len(rays), hits.ctypes.data, int(lights), cull_rel,
+                            cull_abs, threads, stats.ctypes.data)
+    return hits, stats
+
+
+def trace_any(view, rays, lights=False, cull_rel=-1.0, cull_abs=0.0, threads=0):
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    occ = np.empty(len(rays), np.uint8)
+    stats = np.zeros(5, np.uint64)
+    lib().lfo_trace_any(C.addressof(view), rays.ctypes.data, len(rays), occ.ctypes.data, int(lights), cull_rel,
+                        cull_abs, threads, stats.ctypes.data)
+    return occ, stats
+
+
+def render(view, params, first_sample, num_samples, accum=None, want_paths=False, row_stride=1, row_offset=0,
+           threads=0, cull_rel=-1.0, cull_abs=0.0):
+    """Accumulated radiance (H, W, 3) float32 over the samples, in sample order, plus the
+    per-sample path radiance when asked for, and counters [paths, extension rays, node
+    visits, light clamps]."""
+    H, W = params.height, params.width
+    if accum is None:
+        accum = np.zeros((H, W, 3), np.float32)
+    paths = np.zeros((num_samples, H, W, 3), np.float32) if want_paths else None
+    ctr = np.zeros(4, np.uint64)
+    lib().lfo_render(C.addressof(view), C.addressof(params), first_sample, num_samples, accum.ctypes.data,
+                     paths.ctypes.data if paths is not None else None, row_stride, row_offset, threads, cull_rel,
+                     cull_abs, ctr.ctypes.data)
+    return accum, paths, ctr

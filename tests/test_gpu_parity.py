@@ -1,0 +1,184 @@
+"""CUDA path vs the CPU oracle on the same seeded inputs, through the C ABI.
+
+Bars: first-hit instance / packed-triangle ids and hit distances bit-exact; any-hit answers
+identical; per-path radiance bit-exact (the arithmetic contract makes host and device run
+the same IEEE operations), with the 1e-4 relative tolerance of the build plan as the
+reported fallback bar; accumulation buffers identical.
+"""
+import numpy as np
+import pytest
+
+import lavaframe_gb300 as lf
+import oracle
+from tests import scenes
+
+pytestmark = pytest.mark.gpu
+
+PATH_RTOL = 1e-4   # per-path radiance tolerance (relative)
+
+
+def soup_rays(s, n, seed=2, tmax=1e6):
+    a = s.arrays()
+    root = a["nodes"][a["top_level_index"]]
+    return lf.gen_rays(root[0:3], root[3:6], n, seed, tmax)
+
+
+def compare_hits(dev, ref):
+    same_t = dev["t"].view(np.uint32) == ref["t"].view(np.uint32)
+    same = same_t & (dev["instance"] == ref["instance"]) & (dev["prim"] == ref["prim"]) & (dev["light"] == ref["light"])
+    return int((~same).sum())
+
+
+@pytest.mark.parametrize("culling", [True, False])
+def test_closest_hit_ids_bit_exact_on_soup(ctx, culling):
+    s = lf.HostScene().gen_soup(1 << 14, 10, 1).build()
+    ds = ctx.upload(s)
+    if not culling:
+        ds.set_culling(-1.0, 0.0)
+    rays = soup_rays(s, 1 << 18)
+    dev = ctx.trace_closest(ds, rays)
+    ref, _ = oracle.trace_closest(s.view(), rays)
+    mism = compare_hits(dev, ref)
+    assert mism == 0, f"{mism} of {len(rays)} rays differ"
+    assert (dev["prim"] >= 0).mean() > 0.05
+    ds.close()
+
+
+def test_any_hit_matches_on_soup(ctx):
+    s = lf.HostScene().gen_soup(1 << 14, 10, 1).build()
+    ds = ctx.upload(s)
+    rays = soup_rays(s, 1 << 18, seed=3, tmax=30.0)
+    dev = ctx.trace_any(ds, rays)
+    ref, _ = oracle.trace_any(s.view(), rays)
+    assert np.array_equal(dev, ref)
+    assert 0.01 < dev.mean() < 0.99
+    ds.close()
+
+
+def test_traversal_counters_match_oracle_with_culling(ctx):
+    s = lf.HostScene().gen_soup(1 << 12, 10, 1).build()
+    ds = ctx.upload(s)
+    rays = soup_rays(s, 1 << 15)
+    ctx.trace_closest(ds, rays, flags=lf.TRACE_STATS)
+    dstats = ctx.trace_stats()
+    view = s.view()
+    a = s.arrays()
+    extent = float(np.abs(a["nodes"][:, :6]).max())
+    cull_abs = 64 * float(np.spacing(np.float32(extent)))
+    _, ostats = oracle.trace_closest(view, rays, cull_rel=1e-4, cull_abs=cull_abs)
+    # inner-node visits and triangle tests: same visit order, same culling
+    assert dstats[0] == int(ostats[0]) and dstats[1] == int(ostats[1])
+    ds.close()
+
+
+def test_closest_hit_with_lights_on_cornell(ctx):
+    s = scenes.build("cornell")
+    ds = ctx.upload(s)
+    rng = np.random.default_rng(4)
+    n = 1 << 16
+    o = rng.uniform(0.05, 0.95, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = o
+    rays[:, 4:7] = d
+    rays[:, 7] = 1e6
+    dev = ctx.trace_closest(ds, rays, flags=lf.TRACE_LIGHTS)
+    ref, _ = oracle.trace_closest(s.view(), rays, lights=True)
+    assert compare_hits(dev, ref) == 0
+    assert (dev["light"] >= 0).sum() > 0
+    ds.close()
+
+
+def render_both(ctx, s, spp, first=0, flags=0, tile=None, size=None):
+    p = s.render_params()
+    if size:
+        p.width, p.height = size
+    if tile:
+        p.tile_width, p.tile_height = tile
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p, flags)
+    f.render(first, spp)
+    f.sync()
+    dev_acc = f.accum()
+    dev_paths = f.paths(spp) if not tile else None
+    ref_acc, ref_paths, ctr = oracle.render(s.view(), p, first, spp, want_paths=not tile)
+    counters = f.counters()
+    f.close()
+    ds.close()
+    return dev_acc, dev_paths, ref_acc, ref_paths, counters, ctr
+
+
+def assert_paths_match(dev_paths, ref_paths):
+    exact = dev_paths.view(np.uint32) == ref_paths.view(np.uint32)
+    frac_exact = exact.all(axis=-1).mean()
+    rel = np.abs(dev_paths - ref_paths) / np.maximum(np.abs(ref_paths), 1e-6)
+    rel = np.where(np.isfinite(ref_paths) & np.isfinite(dev_paths), rel, 0.0)
+    assert frac_exact == 1.0 or rel.max() <= PATH_RTOL, (frac_exact, float(rel.max()))
+    return frac_exact
+
+
+@pytest.mark.parametrize("name,spp", [("cornell", 4), ("room", 2)])
+def test_path_radiance_matches_oracle(ctx, name, spp):
+    if name == "room":
+        s = lf.HostScene().gen_room(300, 4).build()
+        size = (64, 36)
+    else:
+        s = scenes.build(name)
+        size = None
+    dev_acc, dev_paths, ref_acc, ref_paths, counters, ctr = render_both(ctx, s, spp, size=size)
+    frac = assert_paths_match(dev_paths, ref_paths)
+    assert frac == 1.0
+    assert dev_acc.tobytes() == ref_acc.tobytes()
+    assert counters[1] == ctr[1]          # extension rays traced
+
+
+def test_icospheres_env_transmission_match_oracle(ctx):
+    s = lf.HostScene().gen_icospheres(6, 3, 5, 64, 32).build()
+    p = s.render_params()
+    p.width, p.height = 64, 36
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p)
+    f.render(0, 2)
+    f.sync()
+    dev_paths = f.paths(2)
+    ref_acc, ref_paths, _ = oracle.render(s.view(), p, 0, 2, want_paths=True)
+    assert_paths_match(dev_paths, ref_paths)
+    assert f.accum().tobytes() == ref_acc.tobytes()
+    f.close()
+    ds.close()
+
+
+def test_tiled_render_matches_oracle(ctx):
+    s = scenes.build("cornell")
+    dev_acc, _, ref_acc, _, _, _ = render_both(ctx, s, 2, first=3, tile=(40, 24))
+    assert dev_acc.tobytes() == ref_acc.tobytes()
+
+
+def test_progressive_batches_equal_one_call(ctx):
+    s = scenes.build("cornell")
+    p = s.render_params()
+    ds = ctx.upload(s)
+    f1 = lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM)
+    f1.render(0, 6)
+    f2 = lf.Frame(ctx, ds, p)
+    f2.set_batch(2)
+    f2.render(0, 3)
+    f2.render(3, 3)
+    a1, a2 = f1.accum(), f2.accum()
+    assert a1.tobytes() == a2.tobytes()
+    np.testing.assert_allclose(f1.accum64(), a1, rtol=1e-5, atol=1e-5)
+    for f in (f1, f2):
+        f.close()
+    ds.close()
+
+
+def test_invalid_scene_view_is_rejected(ctx):
+    s = scenes.build("cornell")
+    v = s.view()
+    v.top_level_index = v.num_nodes + 5
+    import ctypes as C
+
+    h = C.c_void_p()
+    st = lf.lib().lf_scene_upload(ctx.h, C.byref(v), C.byref(h))
+    assert st == 1 and not h
