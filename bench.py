@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--rays-log2", type=int, default=24)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     return ap.parse_args()
 
 
@@ -300,21 +302,22 @@ def main():
     value = world * nrays * args.steps / (ms / 1e3) / 1e9
 
     # end to end: page-locked host rays in, hits out, every step
+    e2e_steps = 0 if args.no_e2e else args.steps
     h_rays, h_hits = C.c_void_p(), C.c_void_p()
     ctx._c(L.lf_host_alloc(ctx.h, rays.nbytes, C.byref(h_rays)))
     ctx._c(L.lf_host_alloc(ctx.h, nrays * 16, C.byref(h_hits)))
     C.memmove(h_rays, rays.ctypes.data, rays.nbytes)
     fr = C.cast(h_rays, C.POINTER(C.c_float))
-    for _ in range(args.warmup):
+    for _ in range(args.warmup if e2e_steps else 1):
         ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, nrays, h_hits, 0))
     barrier(world)
     t = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(e2e_steps):
         ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, nrays, h_hits, 0))
     e2e_s = time.perf_counter() - t
     barrier(world)
     e2e_s = max_over_ranks(world, e2e_s)
-    e2e = world * nrays * args.steps / e2e_s / 1e9
+    e2e = world * nrays * e2e_steps / e2e_s / 1e9 if e2e_steps else None
     hits = np.frombuffer((C.c_char * (nrays * 16)).from_address(h_hits.value), dtype=lf.HIT_DTYPE).copy()
 
     # traversal counts for the algorithmic bytes (device counters, same visit order as the oracle)
@@ -327,7 +330,8 @@ def main():
 
         extent = float(np.abs(root[:6]).max())
         cull_abs = 64 * float(np.spacing(np.float32(extent)))
-        cpu_v, cores, sample, cpu_dt, ostats = cpu_baseline(s.view(), rays, args.cpu_seconds, cull_abs)
+        cpu_v, cores, sample, cpu_dt, ostats = cpu_baseline(s.view(), rays, 0.0 if args.no_cpu else args.cpu_seconds,
+                                                            cull_abs)
         # spot check: the sampled rays agree with the oracle bit for bit
         ref_hits, _ = oracle.trace_closest(s.view(), rays[:4096], cull_rel=1e-4, cull_abs=cull_abs)
         extra["parity_spot_check_4096_rays"] = bool(ref_hits.tobytes() == hits[:4096].tobytes())

@@ -231,6 +231,9 @@ lf_status lf_copy_to_host(lf_ctx* c, void* dst, const void* src, size_t bytes);
 lf_status lf_frame_create(lf_ctx* c, lf_scene* sc, const lf_render_params* p, uint32_t flags, lf_frame** out);
 /* Queue samples [first_sample, first_sample + count) (asynchronous). */
 lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count);
+/* One sample of one tile (TiledRenderer::Render, TiledRenderer.cpp:317-352): tile
+ * (tile_x, tile_y) of the frame's tiling, tile_y counted from the bottom as in GL. */
+lf_status lf_frame_render_tile(lf_frame* f, int32_t sample, int32_t tile_x, int32_t tile_y);
 /* Wait for queued work and report device errors. */
 lf_status lf_frame_sync(lf_frame* f);
 /* GetOutputBufferHDR (TiledRenderer.cpp:399-414): accumulated radiance sum, RGB32F,
@@ -247,6 +250,7 @@ lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4]);
 /* Paths processed per wavefront batch (memory/parallelism trade-off); 0 = default. */
 lf_status lf_frame_set_batch(lf_frame* f, int32_t samples_per_batch);
 lf_status lf_frame_release(lf_frame* f);
+
 
 #ifdef __cplusplus
 }

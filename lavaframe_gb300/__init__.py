@@ -79,6 +79,7 @@ _SIG = {
     "lf_copy_to_host": (C.c_int, [_P, _P, _P, C.c_size_t]),
     "lf_frame_create": (C.c_int, [_P, _P, _P, C.c_uint32, C.POINTER(_P)]),
     "lf_frame_render": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "lf_frame_render_tile": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "lf_frame_sync": (C.c_int, [_P]),
     "lf_frame_read_accum": (C.c_int, [_P, _F]),
     "lf_frame_read_accum64": (C.c_int, [_P, C.POINTER(C.c_double)]),

@@ -936,6 +936,24 @@ lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count)
     return LF_OK;
 }
 
+lf_status lf_frame_render_tile(lf_frame* f, int32_t sample, int32_t tile_x, int32_t tile_y)
+{
+    if (!f || sample < 0 || tile_x < 0 || tile_y < 0 || tile_x >= f->numTilesX || tile_y >= f->numTilesY)
+        return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    Params P = f->P;
+    const bool tiledFrames = (f->flags & LF_FRAME_TILED_FRAMES) != 0;
+    P.frameStride = tiledFrames ? f->numTilesX * f->numTilesY : 1;
+    P.tileX = tile_x;
+    P.tileY = tile_y;
+    P.tileOrdinal = tiledFrames ? (f->numTilesY - 1 - tile_y) * f->numTilesX + tile_x : 0;
+    lf_status st = run_batch(f, P, sample, 1);
+    if (st == LF_OK) f->paths += (uint64_t)f->P.tileW * f->P.tileH;
+    return st;
+}
+
 lf_status lf_frame_sync(lf_frame* f)
 {
     if (!f) return LF_ERR_INVALID;
@@ -1038,3 +1056,4 @@ lf_status lf_frame_release(lf_frame* f)
     return LF_OK;
 }
 }
+

@@ -524,7 +524,7 @@ lf_status lf_gen_soup(lf_hscene* s, int32_t instances, int32_t tris, uint64_t se
 }
 
 // Displaced icospheres: `instances` distinct meshes of a level-`level` icosphere
-// (radius 2.5 m, radial displacement 0.1 x fBm of 4 octaves of seeded value noise),
+// (radius 5 m, radial displacement 0.1 x fBm of 4 octaves of seeded value noise),
 // uniform random rotations, translations uniform in a 50 m cube, per-instance Disney
 // materials, and a procedural sky + sun environment of env_w x env_h texels.
 lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint64_t seed, int32_t env_w, int32_t env_h)
@@ -537,7 +537,7 @@ lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint
     std::vector<v3> pts;
     std::vector<int> tri;
     icosphere(level, pts, tri);
-    const float R = 2.5f;
+    const float R = 5.0f;
     std::vector<Vec4> v, n;
     std::vector<v3> disp(pts.size());
     for (int i = 0; i < instances; ++i)
@@ -587,7 +587,7 @@ lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint
         }
     sc.AddHDRData(rgb.data(), env_w, env_h);
     s->options.useEnvMap = true;
-    sc.AddCamera(Vec3(0.f, 20.f, 75.f), Vec3(0.f, 0.f, 0.f), 45.0f);
+    sc.AddCamera(Vec3(0.f, 18.f, 62.f), Vec3(0.f, 0.f, 0.f), 45.0f);
     s->options.resolution = iVec2(1920, 1080);
     s->options.tileWidth = 1920;
     s->options.tileHeight = 1080;
