@@ -251,6 +251,20 @@ lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4]);
 lf_status lf_frame_set_batch(lf_frame* f, int32_t samples_per_batch);
 lf_status lf_frame_release(lf_frame* f);
 
+/* Render without allocating (no counterpart in the reference). For callers that cannot
+ * allocate device memory while rendering - plugin hosts that hand out a fixed arena,
+ * frame loops that forbid allocation, work recorded into CUDA graphs. Accumulates samples
+ * [first_sample, first_sample + count) of `p` into the caller's device buffer `d_accum`
+ * (width*height float4 RGBA32F, row 0 = bottom, A unused; zero it before the first call),
+ * in sample order, with the same results as lf_frame_render.
+ * All wavefront state lives in one fixed device array of the library (about 31.5 MiB per
+ * GPU that loads it, held until exit): one tile (tile_width x tile_height, or the whole
+ * frame) may have at most 131072 pixels, larger tiles are rejected with LF_ERR_INVALID.
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress); make it
+ * before any stream capture. Every call reuses the same array: calls that overlap on the
+ * GPU (other threads, other contexts on the same device) race. Synchronous. */
+lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, int32_t first_sample, int32_t count,
+                            void* d_accum);
 
 #ifdef __cplusplus
 }

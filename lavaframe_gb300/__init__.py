@@ -88,6 +88,7 @@ _SIG = {
     "lf_frame_counters": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "lf_frame_set_batch": (C.c_int, [_P, C.c_int32]),
     "lf_frame_release": (C.c_int, [_P]),
+    "lf_render_noalloc": (C.c_int, [_P, _P, C.c_int32, C.c_int32, _P]),
 }
 
 

@@ -1057,3 +1057,131 @@ lf_status lf_frame_release(lf_frame* f)
 }
 }
 
+// ------------------------------------------------------------------ render without allocating
+// Some callers cannot allocate device memory at render time: plugin hosts that hand the
+// renderer a fixed device arena, real-time loops that forbid allocation inside a frame, and
+// code that records work into a CUDA graph (cudaMalloc is not allowed while a stream is being
+// captured). lf_render_noalloc serves them: all wavefront state lives in one file-scope
+// device array of fixed size, and the accumulation buffer is the caller's.
+namespace
+{
+constexpr long long kNoAllocPaths = 131072;   // path slots = max pixels of one tile
+constexpr size_t kNoAllocAlign = 256;
+constexpr size_t kNoAllocHeader = 256;        // queue sizes, status word, counters
+constexpr size_t noalloc_round(size_t b) { return (b + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+// PathSoA: o, d, T, L, A, rng, info, hit (16 B each), luv (8 B); two int queues; next-event records
+constexpr size_t kNoAllocBytes = kNoAllocHeader + 8 * noalloc_round(kNoAllocPaths * 16) +
+                                 noalloc_round(kNoAllocPaths * 8) + 2 * noalloc_round(kNoAllocPaths * 4) +
+                                 noalloc_round(kNoAllocPaths * sizeof(ShadowRec));
+}
+
+// About 31.5 MiB on every GPU that loads the library, kept until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace
+{
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+// Device address of the scratch array for the current device; resolved once per device.
+lf_status noalloc_base(lf_ctx* c, unsigned char** base)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (c->device < 0 || c->device >= 64) return fail(c, LF_ERR_INVALID, "device index out of range");
+    if (!g_noalloc_addr[c->device])
+    {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(c, e, "cudaGetSymbolAddress(no-alloc scratch)");
+        g_noalloc_addr[c->device] = p;
+    }
+    *base = static_cast<unsigned char*>(g_noalloc_addr[c->device]);
+    return LF_OK;
+}
+}
+
+extern "C" lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, int32_t first_sample, int32_t count,
+                                       void* d_accum)
+{
+    if (!sc || !p || !d_accum || count < 0 || first_sample < 0) return LF_ERR_INVALID;
+    lf_ctx* c = sc->ctx;
+    if (p->width <= 0 || p->height <= 0 || p->max_depth < 0 || p->tile_width < 0 || p->tile_height < 0)
+        return fail(c, LF_ERR_INVALID, "bad render parameters");
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    Params P;
+    fill_params(P, p, sc);
+    const long long tilePix = (long long)P.tileW * P.tileH;
+    if (tilePix > kNoAllocPaths)
+        return fail(c, LF_ERR_INVALID, "lf_render_noalloc: a tile of " + std::to_string(P.tileW) + "x" +
+                                           std::to_string(P.tileH) + " pixels exceeds the fixed capacity of " +
+                                           std::to_string(kNoAllocPaths) + " paths; set tile_width/tile_height");
+    if (count == 0) return LF_OK;
+    unsigned char* base = nullptr;
+    lf_status st = noalloc_base(c, &base);
+    if (st != LF_OK) return st;
+
+    // carve the scratch array
+    unsigned char* q = base + kNoAllocHeader;
+    auto take = [&](size_t bytes) {
+        unsigned char* r = q;
+        q += noalloc_round(bytes);
+        return r;
+    };
+    const size_t N = (size_t)kNoAllocPaths;
+    PathSoA ps;
+    ps.o = (float4*)take(N * 16);
+    ps.d = (float4*)take(N * 16);
+    ps.T = (float4*)take(N * 16);
+    ps.L = (float4*)take(N * 16);
+    ps.A = (float4*)take(N * 16);
+    ps.rng = (uint4*)take(N * 16);
+    ps.info = (int4*)take(N * 16);
+    ps.hit = (float4*)take(N * 16);
+    ps.luv = (float2*)take(N * 8);
+    BounceBuffers bb;
+    bb.queue[0] = (int*)take(N * 4);
+    bb.queue[1] = (int*)take(N * 4);
+    bb.shadow = (ShadowRec*)take(N * sizeof(ShadowRec));
+    bb.count = (int*)(base + 0);
+    bb.shadowCount = (int*)(base + 8);
+    bb.status = (uint32_t*)(base + 12);
+    bb.ctr = (unsigned long long*)(base + 16);
+
+    // the array keeps the previous call's contents: clear sizes, status and counters
+    cudaError_t e = cudaMemsetAsync(base, 0, kNoAllocHeader, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc scratch clear");
+
+    ShadeScene Sv = sc->view;
+    Sv.env.multiplier = P.hdrMultiplier;
+    const int numTilesX = (P.width + P.tileW - 1) / P.tileW, numTilesY = (P.height + P.tileH - 1) / P.tileH;
+    const int spb = (int)std::max(1LL, std::min<long long>(64, kNoAllocPaths / tilePix));
+    for (int s = 0; s < count;)
+    {
+        int n = std::min(spb, count - s);
+        for (int ty = numTilesY - 1; ty >= 0; --ty)
+            for (int tx = 0; tx < numTilesX; ++tx)
+            {
+                P.tileX = tx;
+                P.tileY = ty;
+                long long cap = (long long)n * tilePix;
+                cudaMemsetAsync(bb.count, 0, 2 * sizeof(int), c->stream);
+                int le = launch_generate(Sv, P, ps, first_sample + s, n, bb.queue[0], bb.count, c->stream);
+                for (int b = 0; le == 0 && b < P.maxDepth; ++b) le = launch_bounce(Sv, P, ps, bb, b, cap, c->stream);
+                if (le == 0) le = launch_accumulate(P, ps, n, (float4*)d_accum, nullptr, c->stream);
+                if (le) return cuda_fail(c, (cudaError_t)le, "no-alloc render launch");
+            }
+        s += n;
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc render");
+    uint32_t bits = 0;
+    e = cudaMemcpy(&bits, bb.status, sizeof bits, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc status readback");
+    if (bits)
+    {
+        c->devErrors |= bits;
+        return fail(c, LF_ERR_DEVICE, "device error bits 0x" + std::to_string(bits));
+    }
+    return LF_OK;
+}
