@@ -195,6 +195,8 @@ typedef struct lf_hit
 
 #define LF_TRACE_LIGHTS 0x1   /* include analytic lights, as the LIGHTS shader define */
 #define LF_TRACE_STATS 0x2    /* count node visits / triangle tests (slower) */
+#define LF_TRACE_UNSORTED 0x4 /* trace in input order (no binning by origin cell and octant) */
+#define LF_TRACE_SIMPLE 0x8   /* one thread per ray, no persistent warps */
 
 /* Host buffers: copies rays in, traces, copies hits out (synchronous). */
 lf_status lf_trace_closest(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, lf_hit* hits, uint32_t flags);

@@ -21,6 +21,8 @@ STATUS = {0: "LF_OK", 1: "LF_ERR_INVALID", 2: "LF_ERR_CUDA", 3: "LF_ERR_OOM", 4:
           5: "LF_ERR_TIMEOUT", 6: "LF_ERR_STATE", 7: "LF_ERR_IO", 8: "LF_ERR_BUDGET"}
 TRACE_LIGHTS = 0x1
 TRACE_STATS = 0x2
+TRACE_UNSORTED = 0x4
+TRACE_SIMPLE = 0x8
 FRAME_FP64_ACCUM = 0x1
 FRAME_USE_GRAPH = 0x2
 FRAME_TILED_FRAMES = 0x4

@@ -353,3 +353,197 @@ __device__ __forceinline__ uint32_t any_hit(const DevScene& S, v3 o, v3 d, float
     return err;
 }
 }
+
+namespace lfd
+{
+// Resumable form of `traverse` for persistent kernels: the same state machine and visit
+// order, run for a bounded number of iterations per call so that a warp can refill
+// finished lanes with new rays between calls.
+struct TravState
+{
+    v3 o, d, ro, rd, invd;
+    float t;
+    int code;
+    int sp;
+    int curInst;
+    int hitInst, hitPrim;
+    int steps;
+    uint32_t err;
+    bool meshLevel;
+    int stack[kStackSize];
+};
+
+constexpr int kTravBlasEnd = (int)0x80000000;
+constexpr int kTravEmpty = (int)0x80000001;
+
+__device__ __forceinline__ void trav_init(TravState& s, const DevScene& S, v3 o, v3 d, float t)
+{
+    s.o = o;
+    s.d = d;
+    s.ro = o;
+    s.rd = d;
+    s.invd = 1.0f / d;
+    s.t = t;
+    s.code = S.root;
+    s.sp = 0;
+    s.curInst = -1;
+    s.hitInst = -1;
+    s.hitPrim = -1;
+    s.steps = 0;
+    s.err = 0;
+    s.meshLevel = false;
+}
+
+// Returns true when the traversal has finished (or an error ended it).
+template <bool kAny>
+__device__ __forceinline__ bool trav_run(TravState& s, const DevScene& S, int budget)
+{
+    const bool cull = S.cullRel >= 0.f;
+    for (int it = 0; it < budget; ++it)
+    {
+        if (++s.steps > kMaxTraversalSteps)
+        {
+            s.err |= LF_DEVERR_STEPS;
+            return true;
+        }
+        int code = s.code;
+        if (code == kTravEmpty)
+        {
+            if (s.sp == 0) return true;
+            code = s.stack[--s.sp];
+            if (code == kTravBlasEnd)
+            {
+                s.meshLevel = false;
+                s.ro = s.o;
+                s.rd = s.d;
+                s.invd = 1.0f / s.d;
+                code = kTravEmpty;
+            }
+            s.code = code;
+            continue;
+        }
+        if (code < 0)
+        {
+            const int payload = ~code;
+            if (s.meshLevel)
+            {
+                const int first = payload >> 2, cnt = payload & 3;
+                for (int i = 0; i < cnt; ++i)
+                {
+                    float u, v;
+                    float tt = tri_hit(S.tris + (size_t)(first + i) * 3, s.ro, s.rd, &u, &v);
+                    if (tt >= 0.f && tt < s.t)
+                    {
+                        s.t = tt;
+                        s.hitPrim = first + i;
+                        s.hitInst = s.curInst;
+                        if (kAny) return true;
+                    }
+                }
+                s.code = kTravEmpty;
+            }
+            else
+            {
+                float m[12];
+                int root, mat;
+                load_instance(S.instances + (size_t)payload * 4, m, &root, &mat);
+                if (s.sp >= kStackCap)
+                {
+                    s.err |= LF_DEVERR_STACK;
+                    return true;
+                }
+                s.stack[s.sp++] = kTravBlasEnd;
+                s.ro = xform(m, s.o, 1.0f);
+                s.rd = xform(m, s.d, 0.0f);
+                s.invd = 1.0f / s.rd;
+                s.meshLevel = true;
+                s.curInst = payload;
+                s.code = root;
+            }
+            continue;
+        }
+        const float4* rec = S.nodes + (size_t)code * 4;
+        const float4 f0 = ldg4(rec + 0), f1 = ldg4(rec + 1), f2 = ldg4(rec + 2), f3 = ldg4(rec + 3);
+        float eL, eR;
+        float hL = box_hit(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, s.ro, s.invd, &eL);
+        float hR = box_hit(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, s.ro, s.invd, &eR);
+        if (cull)
+        {
+            const float lim = s.t + s.t * S.cullRel + S.cullAbs;
+            if (eL > lim) hL = -1.0f;
+            if (eR > lim) hR = -1.0f;
+        }
+        const int cL = __float_as_int(f3.x), cR = __float_as_int(f3.y);
+        if (hL > 0.f && hR > 0.f)
+        {
+            int nearC = cL, farC = cR;
+            if (hL > hR)
+            {
+                nearC = cR;
+                farC = cL;
+            }
+            if (s.sp >= kStackCap)
+            {
+                s.err |= LF_DEVERR_STACK;
+                return true;
+            }
+            s.stack[s.sp++] = farC;
+            s.code = nearC;
+        }
+        else if (hL > 0.f)
+            s.code = cL;
+        else if (hR > 0.f)
+            s.code = cR;
+        else
+            s.code = kTravEmpty;
+    }
+    return false;
+}
+
+// Analytic lights of ClosestHit (closest_hit.glsl:13-67): returns the initial t and the
+// light index (or -1).
+__device__ __forceinline__ float lights_closest(const DevScene& S, v3 o, v3 d, float t, int* light)
+{
+    *light = -1;
+    for (int i = 0; i < S.numLights; ++i)
+    {
+        const DevLight& L = S.lights[i];
+        float dd;
+        if (L.type == 0.f)
+        {
+            v3 n(L.normal[0], L.normal[1], L.normal[2]);
+            if (lfc::dot(n, d) > 0.f) continue;
+            dd = rect_intersect(L, o, d);
+            if (dd < 0.f) dd = kInfinity;
+            if (dd < t) { t = dd; *light = i; }
+        }
+        if (L.type == 1.f)
+        {
+            dd = sphere_intersect(L, o, d);
+            if (dd < 0.f) dd = kInfinity;
+            if (dd < t) { t = dd; *light = i; }
+        }
+    }
+    return t;
+}
+
+// Analytic lights of AnyHit (anyhit.glsl:15-50).
+__device__ __forceinline__ bool lights_any(const DevScene& S, v3 o, v3 d, float maxDist)
+{
+    for (int i = 0; i < S.numLights; ++i)
+    {
+        const DevLight& L = S.lights[i];
+        if (L.type == 0.f)
+        {
+            float dd = rect_intersect(L, o, d);
+            if (dd > 0.f && dd < maxDist) return true;
+        }
+        if (L.type == 1.f)
+        {
+            float dd = sphere_intersect(L, o, d);
+            if (dd > 0.f && dd < maxDist) return true;
+        }
+    }
+    return false;
+}
+}

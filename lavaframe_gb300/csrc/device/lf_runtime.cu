@@ -30,6 +30,12 @@ struct lf_ctx
     void* scratchOut = nullptr;
     size_t scratchOutBytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // scratch of the binned ray queries
+    uint32_t* binKeys = nullptr;
+    int* binPerm = nullptr;
+    size_t binCap = 0;
+    uint32_t* binHist = nullptr;
+    unsigned long long* binNext = nullptr;
 };
 
 struct lf_scene
@@ -50,6 +56,7 @@ struct lf_scene
     DevMaterial* d_materials = nullptr;
     int numMaterials = 0;
     std::vector<int> meshNodeMap;   // reference index -> device record (mesh levels), -1 otherwise
+    float boundsLo[3] = {0, 0, 0}, boundsHi[3] = {0, 0, 0};   // instance-level root box
 };
 
 struct lf_frame
@@ -166,6 +173,10 @@ void lf_ctx_destroy(lf_ctx* c)
     cudaFree(c->d_stats);
     cudaFree(c->scratchRays);
     cudaFree(c->scratchOut);
+    cudaFree(c->binKeys);
+    cudaFree(c->binPerm);
+    cudaFree(c->binHist);
+    cudaFree(c->binNext);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -582,6 +593,11 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     }
     sc->numRefNodes = v->num_nodes;
     sc->topLevelIndex = v->top_level_index;
+    for (int k = 0; k < 3; ++k)
+    {
+        sc->boundsLo[k] = nodes[v->top_level_index].bmin[k];
+        sc->boundsHi[k] = nodes[v->top_level_index].bmax[k];
+    }
     sc->d_nodes = d_nodes;
     sc->nodeCapacity = recs.size() / 4;
     sc->d_instances = d_inst;
@@ -649,6 +665,38 @@ lf_status lf_scene_set_culling(lf_scene* sc, float rel, float abs_margin)
 size_t lf_scene_device_bytes(const lf_scene* sc) { return sc ? sc->bytes : 0; }
 
 // ------------------------------------------------------------------ ray queries
+}   // extern "C"
+
+namespace
+{
+// Grows the binning scratch (keys, permutation, bin counters, fetch counter) of a context.
+lf_status ensure_bin_scratch(lf_ctx* c, long long n)
+{
+    if (!c->binHist)
+    {
+        cudaError_t e = cudaMalloc((void**)&c->binHist, sizeof(uint32_t) * (size_t)trace_bins());
+        if (e == cudaSuccess) e = cudaMalloc((void**)&c->binNext, sizeof(unsigned long long));
+        if (e != cudaSuccess) return cuda_fail(c, e, "binning scratch");
+    }
+    if ((size_t)n > c->binCap)
+    {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->binKeys);
+        cudaFree(c->binPerm);
+        c->binKeys = nullptr;
+        c->binPerm = nullptr;
+        c->binCap = 0;
+        cudaError_t e = cudaMalloc((void**)&c->binKeys, sizeof(uint32_t) * (size_t)n);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&c->binPerm, sizeof(int) * (size_t)n);
+        if (e != cudaSuccess) return cuda_fail(c, e, "binning scratch");
+        c->binCap = (size_t)n;
+    }
+    return LF_OK;
+}
+}
+
+extern "C" {
+
 lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_hits, uint32_t flags)
 {
     if (!c || !sc || (n > 0 && (!d_rays || !d_hits)) || n < 0) return LF_ERR_INVALID;
@@ -657,7 +705,17 @@ lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, i
     cudaSetDevice(c->device);
     bool stats = (flags & LF_TRACE_STATS) != 0;
     if (stats) cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream);
-    int e = launch_trace_closest(sc->view.trav, (const float4*)d_rays, n, (int4*)d_hits, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+    int e;
+    if (!stats && !(flags & LF_TRACE_SIMPLE))
+    {
+        lf_status bs = ensure_bin_scratch(c, n);
+        if (bs != LF_OK) return bs;
+        e = launch_trace_binned(sc->view.trav, (const float4*)d_rays, n, d_hits, false, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+                                sc->boundsLo, sc->boundsHi, !(flags & LF_TRACE_UNSORTED), c->binKeys, c->binHist,
+                                c->binPerm, c->binNext, c->d_status, c->stream);
+    }
+    else
+        e = launch_trace_closest(sc->view.trav, (const float4*)d_rays, n, (int4*)d_hits, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
                                  stats, c->d_status, c->d_stats, c->stream);
     if (e) return cuda_fail(c, (cudaError_t)e, "trace launch");
     return LF_OK;
@@ -671,7 +729,17 @@ lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64
     cudaSetDevice(c->device);
     bool stats = (flags & LF_TRACE_STATS) != 0;
     if (stats) cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream);
-    int e = launch_trace_any(sc->view.trav, (const float4*)d_rays, n, (uint8_t*)d_occ, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+    int e;
+    if (!stats && !(flags & LF_TRACE_SIMPLE))
+    {
+        lf_status bs = ensure_bin_scratch(c, n);
+        if (bs != LF_OK) return bs;
+        e = launch_trace_binned(sc->view.trav, (const float4*)d_rays, n, d_occ, true, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
+                                sc->boundsLo, sc->boundsHi, !(flags & LF_TRACE_UNSORTED), c->binKeys, c->binHist,
+                                c->binPerm, c->binNext, c->d_status, c->stream);
+    }
+    else
+        e = launch_trace_any(sc->view.trav, (const float4*)d_rays, n, (uint8_t*)d_occ, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
                              stats, c->d_status, c->d_stats, c->stream);
     if (e) return cuda_fail(c, (cudaError_t)e, "trace launch");
     return LF_OK;

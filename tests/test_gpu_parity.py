@@ -44,6 +44,21 @@ def test_closest_hit_ids_bit_exact_on_soup(ctx, culling):
     ds.close()
 
 
+@pytest.mark.parametrize("flags", [lf.TRACE_SIMPLE, lf.TRACE_UNSORTED, 0])
+def test_trace_variants_agree_with_oracle(ctx, flags):
+    """Per-thread, persistent, and binned+persistent traversal give the same hits."""
+    s = lf.HostScene().gen_soup(1 << 12, 10, 5).build()
+    ds = ctx.upload(s)
+    rays = soup_rays(s, 100003, seed=9)          # not a multiple of the warp size
+    dev = ctx.trace_closest(ds, rays, flags=flags)
+    ref, _ = oracle.trace_closest(s.view(), rays)
+    assert compare_hits(dev, ref) == 0
+    occ = ctx.trace_any(ds, rays, flags=flags)
+    ref_occ, _ = oracle.trace_any(s.view(), rays)
+    assert np.array_equal(occ, ref_occ)
+    ds.close()
+
+
 def test_any_hit_matches_on_soup(ctx):
     s = lf.HostScene().gen_soup(1 << 14, 10, 1).build()
     ds = ctx.upload(s)
