@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
+    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full"],
+                    help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
 
 
@@ -231,15 +233,15 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which):
+def render_extra(ctx, which, spp=None):
     import lavaframe_gb300 as lf
 
     if which == "c1":
         s = lf.HostScene().gen_cornell(256, 256).build()
-        spp = 64
+        spp = spp or 64
     else:
-        s = lf.HostScene().gen_icospheres(13, 6, 3, 1024, 512).build()
-        spp = 16
+        s = lf.HostScene().gen_icospheres(64 if which == "c3full" else 13, 6, 3, 1024, 512).build()
+        spp = spp or 16
     p = s.render_params()
     ds = ctx.upload(s)
     f = lf.Frame(ctx, ds, p)
@@ -274,6 +276,13 @@ def main():
     b.build_core()
     b.build_oracle()
     ctx = lf.Context(local)
+    if args.workload != "microbench":
+        r = render_extra(ctx, args.workload)
+        if rank == 0:
+            print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
+                              "unit": "rays/s", "detail": r}), flush=True)
+        ctx.close()
+        return
     s, t_gen, t_build = build_soup(args.instances_log2)
     nrays = 1 << args.rays_log2
     rays, root = soup_rays(s, nrays)

@@ -39,6 +39,7 @@ struct BounceBuffers
     int* shadowCount;
     uint32_t* status;
     unsigned long long* ctr;   // [0] paths, [1] extension rays, [2] shadow rays, [3] light clamps
+    unsigned long long* fetch; // [2] work counters of the persistent extend / shadow kernels
 };
 
 int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,

@@ -4,6 +4,7 @@
 // precomputation and matrix inverses are part of the arithmetic contract.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -878,6 +879,7 @@ lf_status alloc_paths(lf_frame* f, long long cap)
     A(&f->bb.count, 2);
     A(&f->bb.shadow, cap);
     A(&f->bb.shadowCount, 1);
+    A(&f->bb.fetch, 2);
     if (e != cudaSuccess)
     {
         free_frame_buffers(f);
@@ -964,9 +966,15 @@ lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
     cudaMemsetAsync(f->bb.count, 0, 2 * sizeof(int), c->stream);
     int e = launch_generate(Sv, P, f->ps, firstSample, n, f->bb.queue[0], f->bb.count, c->stream);
     if (e) return cuda_fail(c, (cudaError_t)e, "generate launch");
+    BounceBuffers bb = f->bb;
+    // Queue order is already coherent (camera rays in pixel order, survivors compacted in
+    // order), and one thread per queued ray measured faster than persistent warps on the
+    // icosphere scenes; LF_WAVEFRONT_PERSISTENT=1 selects the persistent extend/shadow kernels.
+    static const bool persistent = std::getenv("LF_WAVEFRONT_PERSISTENT") != nullptr;
+    if (!persistent) bb.fetch = nullptr;
     for (int b = 0; b < P.maxDepth; ++b)
     {
-        e = launch_bounce(Sv, P, f->ps, f->bb, b, cap, c->stream);
+        e = launch_bounce(Sv, P, f->ps, bb, b, cap, c->stream);
         if (e) return cuda_fail(c, (cudaError_t)e, "bounce launch");
     }
     e = launch_accumulate(P, f->ps, n, f->accum, f->accum64, c->stream);
@@ -1215,6 +1223,7 @@ extern "C" lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, 
     bb.shadowCount = (int*)(base + 8);
     bb.status = (uint32_t*)(base + 12);
     bb.ctr = (unsigned long long*)(base + 16);
+    bb.fetch = (unsigned long long*)(base + 48);
 
     // the array keeps the previous call's contents: clear sizes, status and counters
     cudaError_t e = cudaMemsetAsync(base, 0, kNoAllocHeader, c->stream);
