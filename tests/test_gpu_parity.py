@@ -197,3 +197,31 @@ def test_invalid_scene_view_is_rejected(ctx):
     h = C.c_void_p()
     st = lf.lib().lf_scene_upload(ctx.h, C.byref(v), C.byref(h))
     assert st == 1 and not h
+
+
+@pytest.mark.parametrize("name", ["cornell", "cornell_lights", "cornell_textures", "room", "icospheres",
+                                  "icospheres_constbg_tiled", "icospheres_lens"])
+def test_gpu_paths_equal_reference_shader(ctx, name):
+    """Device paths against the reference GLSL shader compiled for the CPU (golden vectors)."""
+    import json
+
+    from tests.conftest import ROOT
+    from tests.golden import cases
+
+    gold = np.load(ROOT / "tests" / "golden" / "shader_paths.npz")[name]
+    a, p, extras = cases.build(name)
+    view, keep = cases.make_view(a, extras)
+    ds = lf.DeviceScene(ctx, view)
+    f = lf.Frame(ctx, ds, p)
+    spp = gold.shape[0]
+    f.render(0, spp)
+    f.sync()
+    if p.tile_width:
+        got = f.accum()[None]
+        gold = gold.sum(axis=0, keepdims=True)
+    else:
+        got = f.paths(spp)
+    same = np.all((got == gold) | (np.isnan(got) & np.isnan(gold)), axis=-1)
+    f.close()
+    ds.close()
+    assert same.all(), f"{(~same).sum()} of {same.size} paths differ"
