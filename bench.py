@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
+    ap.add_argument("--spp-batch", type=int, default=0, help="samples per wavefront batch of the render workloads")
+    ap.add_argument("--frame-flags", type=int, default=0, help="lf_frame flags of the render workloads (8 = per-batch)")
+    ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
+    ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (0/512/768)")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
@@ -233,7 +237,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which, spp=None):
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0):
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -244,7 +248,9 @@ def render_extra(ctx, which, spp=None):
         spp = spp or 16
     p = s.render_params()
     ds = ctx.upload(s)
-    f = lf.Frame(ctx, ds, p)
+    f = lf.Frame(ctx, ds, p, flags)
+    if spp_batch:
+        f.set_batch(spp_batch)
     f.render(0, 1)
     f.sync()
     f.reset()
@@ -276,8 +282,10 @@ def main():
     b.build_core()
     b.build_oracle()
     ctx = lf.Context(local)
+    if args.engine_slots or args.shade_cap:
+        ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap)
     if args.workload != "microbench":
-        r = render_extra(ctx, args.workload)
+        r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags)
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)
@@ -354,9 +362,9 @@ def main():
             pj = json.loads(prof.read_text())
             traffic = pj.get("dram_bytes_per_ray", 0) * nrays
         if not args.no_extras:
-            for w in ("c1", "c3_1m"):
+            for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8)):
                 try:
-                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3")
+                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags)
                 except Exception as e:  # reported, not fatal for the headline
                     extra[w] = {"error": str(e)}
         extra.update({"scene_build_s": t_build, "scene_generate_s": t_gen, "hit_fraction": float((hits["prim"] >= 0).mean()),

@@ -225,10 +225,16 @@ lf_status lf_copy_to_host(lf_ctx* c, void* dst, const void* src, size_t bytes);
  * (TiledRenderer.cpp:317-554) without the GL passes. Samples accumulate in sample order,
  * so results do not depend on how calls are batched. */
 #define LF_FRAME_FP64_ACCUM 0x1   /* also accumulate in double precision */
-#define LF_FRAME_USE_GRAPH 0x2    /* replay the bounce loop as a CUDA graph */
+#define LF_FRAME_USE_GRAPH 0x2    /* per-batch pipeline: record each batch (generate, bounces,
+                                     accumulate) as a CUDA graph and replay it; the engine
+                                     pipeline always replays graph-captured steps */
 #define LF_FRAME_TILED_FRAMES 0x4 /* TiledRenderer RNG keying: the shader `frame` advances per
                                      tile (TiledRenderer.cpp:486-501): frame = frame_base +
                                      sample * tiles + tile, tiles counted from the top row */
+#define LF_FRAME_PER_BATCH 0x8    /* lf_frame_render runs bounce-synchronous batches (every
+                                     path of a batch advances one bounce per launch) instead of
+                                     the context's multi-job engine (paths regenerate in a fixed
+                                     slot pool). Results are identical; only speed differs. */
 
 lf_status lf_frame_create(lf_ctx* c, lf_scene* sc, const lf_render_params* p, uint32_t flags, lf_frame** out);
 /* Queue samples [first_sample, first_sample + count) (asynchronous). */
@@ -249,9 +255,20 @@ lf_status lf_frame_reset(lf_frame* f);
 /* Counters since creation/reset: [0] camera paths, [1] extension rays, [2] shadow rays,
  * [3] light-index clamps (rand() == 1). */
 lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4]);
-/* Paths processed per wavefront batch (memory/parallelism trade-off); 0 = default. */
+/* Samples per wavefront batch (per-batch pipeline) or per engine pass (memory/parallelism
+ * trade-off); 0 = default. */
 lf_status lf_frame_set_batch(lf_frame* f, int32_t samples_per_batch);
 lf_status lf_frame_release(lf_frame* f);
+
+/* Engine of the context (no counterpart in the reference; the reference renders one tile per
+ * GL draw). `slots` = path slots in the pool (0 keeps the current pool), block sizes of the
+ * extend / shade / shadow kernels (0 = default 128; multiples of 32 up to 1024, shade up to
+ * 256), and the register cap of the shade kernel as the threads per SM it must fit (0 = none,
+ * 512 or 768). Fails with LF_ERR_STATE while passes are in flight. */
+lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend, int32_t block_shade,
+                                  int32_t block_shadow, int32_t shade_threads_per_sm);
+/* Current pool size and device bytes of the engine (0, 0 before first use). */
+lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 
 /* Render without allocating (no counterpart in the reference). For callers that cannot
  * allocate device memory while rendering - plugin hosts that hand out a fixed arena,

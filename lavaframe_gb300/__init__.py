@@ -26,6 +26,7 @@ TRACE_SIMPLE = 0x8
 FRAME_FP64_ACCUM = 0x1
 FRAME_USE_GRAPH = 0x2
 FRAME_TILED_FRAMES = 0x4
+FRAME_PER_BATCH = 0x8
 
 # symbol -> (restype, argtypes); kept in the same order as include/lavaframe_gb300.h
 _P = C.c_void_p
@@ -63,6 +64,8 @@ _SIG = {
     "lf_ctx_sync": (C.c_int, [_P]),
     "lf_ctx_timer_start": (C.c_int, [_P]),
     "lf_ctx_timer_stop": (C.c_int, [_P, _F]),
+    "lf_ctx_configure_engine": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "lf_ctx_engine_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "lf_scene_upload": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_scene_update_instances": (C.c_int, [_P, _P]),
     "lf_scene_release": (C.c_int, [_P]),
@@ -333,6 +336,17 @@ class Context:
 
     def device_errors(self):
         return lib().lf_ctx_device_errors(self.h)
+
+    def configure_engine(self, slots=0, block_extend=0, block_shade=0, block_shadow=0, shade_threads_per_sm=0):
+        """Pool size, kernel block sizes and shade register cap of the multi-job engine
+        (0 = keep the pool / default)."""
+        self._c(lib().lf_ctx_configure_engine(self.h, slots, block_extend, block_shade, block_shadow,
+                                              shade_threads_per_sm))
+
+    def engine_info(self):
+        slots, nbytes = C.c_int64(), C.c_int64()
+        self._c(lib().lf_ctx_engine_info(self.h, C.byref(slots), C.byref(nbytes)))
+        return {"slots": slots.value, "device_bytes": nbytes.value}
 
     def upload(self, host_scene: HostScene) -> "DeviceScene":
         v = host_scene.view()

@@ -86,6 +86,75 @@ __device__ __forceinline__ float box_hit(float bminx, float bminy, float bminz, 
     return (t1 >= t0) ? (t0 > 0.f ? t0 : t1) : -1.0f;
 }
 
+// The exact test for rays with a zero, denormal or non-finite inverse direction component:
+// their slab values can be NaN or infinite, so the entry is no lower bound of the hit distance
+// and such rays are never culled.
+__device__ __forceinline__ float box_hit_exact(float bminx, float bminy, float bminz, float bmaxx, float bmaxy,
+                                               float bmaxz, v3 o, v3 invd, float* entry)
+{
+    const float h = box_hit(bminx, bminy, bminz, bmaxx, bmaxy, bmaxz, o, invd, entry);
+    *entry = 0.f;
+    return h;
+}
+
+// Three-input min / max (sm_100 and later).
+__device__ __forceinline__ float fmin3_hw(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+__device__ __forceinline__ float fmax3_hw(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// The same test for rays whose inverse direction is finite and non-zero in every component.
+// Then no slab value is NaN (no 0 * inf), and the hardware min / max agree with the GLSL
+// select forms except for the sign of a zero result, which no comparison below can see
+// (t0 and t1 are only compared with each other and with zero, the returned value only with
+// zero and the sibling's value, the entry only with a positive limit). Rays with a zero or
+// denormal direction component keep the exact form.
+__device__ __forceinline__ float box_hit_fast(float bminx, float bminy, float bminz, float bmaxx, float bmaxy,
+                                              float bmaxz, v3 o, v3 invd, float* entry)
+{
+    float fx = (bmaxx - o.x) * invd.x, fy = (bmaxy - o.y) * invd.y, fz = (bmaxz - o.z) * invd.z;
+    float nx = (bminx - o.x) * invd.x, ny = (bminy - o.y) * invd.y, nz = (bminz - o.z) * invd.z;
+    float t1 = fmin3_hw(fmaxf(fx, nx), fmaxf(fy, ny), fmaxf(fz, nz));
+    float t0 = fmax3_hw(fminf(fx, nx), fminf(fy, ny), fminf(fz, nz));
+    *entry = fmaxf(t0, 0.f);
+    return (t1 >= t0) ? (t0 > 0.f ? t0 : t1) : -1.0f;
+}
+
+__device__ __forceinline__ bool fast_inv(float x) { return fabsf(x) < 3.0e38f && x != 0.f; }   // false for NaN
+
+// Inverse direction and whether the fast box test applies to it.
+__device__ __forceinline__ v3 inv_dir(v3 d, bool* fast)
+{
+    v3 inv = 1.0f / d;
+    *fast = fast_inv(inv.x) && fast_inv(inv.y) && fast_inv(inv.z);
+    return inv;
+}
+
+// Both child boxes of an inner-node record.
+__device__ __forceinline__ void box_pair(float4 f0, float4 f1, float4 f2, v3 o, v3 invd, bool fast, float* hL,
+                                         float* hR, float* eL, float* eR)
+{
+    if (fast)
+    {
+        *hL = box_hit_fast(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o, invd, eL);
+        *hR = box_hit_fast(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o, invd, eR);
+    }
+    else
+    {
+        *hL = box_hit_exact(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, o, invd, eL);
+        *hR = box_hit_exact(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, o, invd, eR);
+    }
+}
+
 // Moller-Trumbore as in closest_hit.glsl:119-134: returns t (= uvt.z) when all of
 // (u, v, t, 1-u-v) are >= 0, else a negative value. u, v returned for barycentrics.
 __device__ __forceinline__ float tri_hit(const float4* tri, v3 o, v3 d, float* pu, float* pv)
@@ -184,7 +253,8 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
     bool meshLevel = false;
     int curInst = -1;
     v3 ro = o, rd = d;
-    v3 invd = 1.0f / rd;
+    bool fast;
+    v3 invd = inv_dir(rd, &fast);
     float m[12];
     uint32_t err = 0;
     const bool cull = S.cullRel >= 0.f;
@@ -203,7 +273,7 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
                 meshLevel = false;
                 ro = o;
                 rd = d;
-                invd = 1.0f / rd;
+                invd = inv_dir(rd, &fast);
                 code = kEmpty;
             }
             continue;
@@ -245,7 +315,7 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
                 stack[sp++] = kBlasEnd;
                 ro = xform(m, o, 1.0f);
                 rd = xform(m, d, 0.0f);
-                invd = 1.0f / rd;
+                invd = inv_dir(rd, &fast);
                 meshLevel = true;
                 curInst = inst;
                 code = root;
@@ -255,9 +325,8 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
         const float4* rec = S.nodes + (size_t)code * 4;
         const float4 f0 = ldg4(rec + 0), f1 = ldg4(rec + 1), f2 = ldg4(rec + 2), f3 = ldg4(rec + 3);
         if (kStats) st->nodes++;
-        float eL, eR;
-        float hL = box_hit(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, ro, invd, &eL);
-        float hR = box_hit(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, ro, invd, &eR);
+        float eL, eR, hL, hR;
+        box_pair(f0, f1, f2, ro, invd, fast, &hL, &hR, &eL, &eR);
         if (cull)
         {
             const float lim = t + t * S.cullRel + S.cullAbs;
@@ -370,6 +439,7 @@ struct TravState
     int steps;
     uint32_t err;
     bool meshLevel;
+    bool fast;
     int stack[kStackSize];
 };
 
@@ -382,7 +452,7 @@ __device__ __forceinline__ void trav_init(TravState& s, const DevScene& S, v3 o,
     s.d = d;
     s.ro = o;
     s.rd = d;
-    s.invd = 1.0f / d;
+    s.invd = inv_dir(d, &s.fast);
     s.t = t;
     s.code = S.root;
     s.sp = 0;
@@ -416,7 +486,7 @@ __device__ __forceinline__ bool trav_run(TravState& s, const DevScene& S, int bu
                 s.meshLevel = false;
                 s.ro = s.o;
                 s.rd = s.d;
-                s.invd = 1.0f / s.d;
+                s.invd = inv_dir(s.d, &s.fast);
                 code = kTravEmpty;
             }
             s.code = code;
@@ -455,7 +525,7 @@ __device__ __forceinline__ bool trav_run(TravState& s, const DevScene& S, int bu
                 s.stack[s.sp++] = kTravBlasEnd;
                 s.ro = xform(m, s.o, 1.0f);
                 s.rd = xform(m, s.d, 0.0f);
-                s.invd = 1.0f / s.rd;
+                s.invd = inv_dir(s.rd, &s.fast);
                 s.meshLevel = true;
                 s.curInst = payload;
                 s.code = root;
@@ -464,9 +534,8 @@ __device__ __forceinline__ bool trav_run(TravState& s, const DevScene& S, int bu
         }
         const float4* rec = S.nodes + (size_t)code * 4;
         const float4 f0 = ldg4(rec + 0), f1 = ldg4(rec + 1), f2 = ldg4(rec + 2), f3 = ldg4(rec + 3);
-        float eL, eR;
-        float hL = box_hit(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, s.ro, s.invd, &eL);
-        float hR = box_hit(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, s.ro, s.invd, &eR);
+        float eL, eR, hL, hR;
+        box_pair(f0, f1, f2, s.ro, s.invd, s.fast, &hL, &hR, &eL, &eR);
         if (cull)
         {
             const float lim = s.t + s.t * S.cullRel + S.cullAbs;

@@ -1,0 +1,419 @@
+// Kernels of the persistent multi-job wavefront engine (tables and step order in lf_engine.h).
+// The per-path work is the same code as the per-batch frame kernels (lf_pathops.cuh); only
+// the bookkeeping differs: paths find their job through info.w, finished paths hand their
+// slot to a new path, and pass completion is counted on the device.
+#include "lf_engine.h"
+#include "lf_pathops.cuh"
+
+namespace lfd
+{
+using namespace pathops;
+
+namespace
+{
+__device__ __forceinline__ int job_of(int w) { return (int)((unsigned)w >> kPassRingBits); }
+__device__ __forceinline__ int ring_of(int w) { return w & (kPassRing - 1); }
+
+// Pass completion counting: warp leaders add into a small shared table keyed by ring
+// entry, then one global atomic per distinct entry of the block. Every thread must call.
+struct DoneTable
+{
+    int key[8];
+    unsigned cnt[8];
+};
+
+__device__ __forceinline__ void count_done_block(int ring, unsigned long long* passDone, DoneTable& t)
+{
+    if (threadIdx.x < 8)
+    {
+        t.key[threadIdx.x] = -1;
+        t.cnt[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    const unsigned act = __ballot_sync(kFull, ring >= 0);
+    if (ring >= 0)
+    {
+        const unsigned peers = __match_any_sync(act, ring);
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        {
+            bool placed = false;
+            for (int k = 0; k < 8 && !placed; ++k)
+            {
+                const int e = (ring + k) & 7;
+                const int old = atomicCAS(&t.key[e], -1, ring);
+                if (old == -1 || old == ring)
+                {
+                    atomicAdd(&t.cnt[e], (unsigned)__popc(peers));
+                    placed = true;
+                }
+            }
+            if (!placed) atomicAdd(&passDone[ring], (unsigned long long)__popc(peers));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && t.key[threadIdx.x] >= 0 && t.cnt[threadIdx.x])
+        atomicAdd(&passDone[t.key[threadIdx.x]], (unsigned long long)t.cnt[threadIdx.x]);
+    __syncthreads();
+}
+
+// Largest pass g in [lo, hi) with pathBase <= id (passes are in increasing pathBase order).
+__device__ __forceinline__ unsigned long long find_pass(const EnginePass* passes, unsigned long long id,
+                                                        unsigned long long lo, unsigned long long hi)
+{
+    while (hi - lo > 1)
+    {
+        const unsigned long long mid = lo + ((hi - lo) >> 1);
+        if (passes[mid & (kPassRing - 1)].pathBase <= id) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+}
+
+// ------------------------------------------------------------------ init / append / reset
+__global__ void engine_init_kernel(EngineBuffers b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
+    {
+        b.ps.info[i] = make_int4(0, 0, 0, -1);
+        b.done[0][i] = i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        b.ctl->doneCount[0] = b.cap;
+        b.ctl->doneCount[1] = 0;
+        b.ctl->active = 0;
+        b.ctl->count[0] = 0;
+        b.ctl->count[1] = 0;
+        b.ctl->shadowCount = 0;
+    }
+}
+
+__global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, unsigned long long numPasses)
+{
+    EngineCtl* c = b.ctl;
+    unsigned long long next = c->next < c->total ? c->next : c->total;
+    c->next = next;
+    c->total = total;
+    c->numPasses = numPasses;
+    unsigned long long lo = c->passLo;
+    while (lo + 1 < numPasses)
+    {
+        const EnginePass& q = b.passes[lo & (kPassRing - 1)];
+        if (q.pathBase + q.numPaths > next) break;
+        ++lo;
+    }
+    c->passLo = lo;
+}
+
+__global__ void engine_reset_kernel(EngineCtl* c, int parity)
+{
+    c->doneCount[parity] = 0;
+    c->shadowCount = 0;
+    c->count[parity ^ 1] = 0;
+}
+
+// ------------------------------------------------------------------ finish
+// Writes out the radiance of every finished path, then gives each freed slot the next
+// unissued path id (camera ray of renderer.glsl:27-62) and queues it for extension. Slots
+// left without work wait on the other done list for a later append.
+template <bool kOne>
+__global__ void engine_finish_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    __shared__ int smem[33];
+    __shared__ unsigned long long sFirst;
+    __shared__ DoneTable table;
+    EngineCtl* ctl = b.ctl;
+    const int n = ctl->doneCount[parity];
+    const int* done = b.done[parity];
+    const unsigned long long total = ctl->total;
+    const unsigned long long plo = ctl->passLo, phi = ctl->numPasses;
+    const bool work = ctl->next < total;
+    int* q = b.queue[parity];
+    int* qc = &ctl->count[parity];
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    // block-uniform loop: block_push synchronises the block
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        const int i = base + threadIdx.x;
+        const int slot = i < n ? done[i] : -1;
+        int ring = -1;
+        if (slot >= 0)
+        {
+            const int w = reinterpret_cast<const int*>(b.ps.info)[4 * slot + 3];
+            if (w >= 0)
+            {
+                ring = ring_of(w);
+                const int local = reinterpret_cast<const int*>(b.ps.info)[4 * slot];
+                b.passes[ring].radiance[local] = b.ps.L[slot];
+            }
+        }
+        count_done_block(ring, b.passDone, table);
+
+        bool started = false, push = false;
+        if (work)
+        {
+            // one id range per block: warp offsets in smem, one atomic on `next`
+            const unsigned need = __ballot_sync(kFull, slot >= 0);
+            const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            if (lane == 0) smem[warp] = __popc(need);
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                int tot = 0;
+                for (int w = 0; w < nw; ++w)
+                {
+                    const int c = smem[w];
+                    smem[w] = tot;
+                    tot += c;
+                }
+                sFirst = tot ? atomicAdd(&ctl->next, (unsigned long long)tot) : 0ull;
+            }
+            __syncthreads();
+            const unsigned long long first = sFirst + (unsigned long long)smem[warp];
+            __syncthreads();
+            if (slot >= 0)
+            {
+                const unsigned long long id = first + __popc(need & ((1u << lane) - 1u));
+                if (id < total)
+                {
+                    const unsigned long long g = find_pass(b.passes, id, plo, phi);
+                    const int r = (int)(g & (kPassRing - 1));
+                    const EnginePass& Q = b.passes[r];
+                    const Params& P = kOne ? one.P : b.jobs[Q.job].P;
+                    const int local = (int)(id - Q.pathBase);   // passes hold < 2^31 paths
+                    const int visPix = Q.visW * Q.visH;
+                    const int s = local / visPix;
+                    const int lp = local - s * visPix;
+                    const int ly = lp / Q.visW, lx = lp - ly * Q.visW;
+                    b.ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    b.ps.info[slot] = make_int4(local, 0, 0, r | (Q.job << kPassRingBits));
+                    gen_path(P, Q.tileX, Q.tileY, Q.tileOrdinal, Q.firstSample + s, lx, ly, b.ps, slot);
+                    started = true;
+                    push = P.maxDepth > 0;   // depth 0: the path ends with zero radiance
+                }
+            }
+        }
+        if (slot >= 0 && !started && ring >= 0)
+            reinterpret_cast<int*>(b.ps.info)[4 * slot + 3] = -1;   // idle until the next append
+        block_push(push, slot, q, qc, b.cap, b.status, smem);
+        block_push(slot >= 0 && !push, slot, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
+        // active += started - written out, one atomic per warp
+        const int delta = __popc(__ballot_sync(kFull, started)) - __popc(__ballot_sync(kFull, ring >= 0));
+        if (lane == 0 && delta != 0) atomicAdd(&ctl->active, delta);
+    }
+}
+
+// ------------------------------------------------------------------ extend / shade / shadow
+template <bool kOne>
+__global__ void engine_extend_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    const int n = b.ctl->count[parity];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr[1], (unsigned long long)n);
+    const int* q = b.queue[parity];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int p = q[i];
+        const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
+        Hit h;
+        uint32_t err;
+        if constexpr (kOne)
+            err = closest_hit<false>(one.S.trav, f3(o4), f3(d4), kInfinity, one.P.useLights != 0, &h, nullptr);
+        else
+        {
+            const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
+            const EngineJob& J = b.jobs[job_of(w)];
+            const DevScene T = J.S.trav;
+            err = closest_hit<false>(T, f3(o4), f3(d4), kInfinity, J.P.useLights != 0, &h, nullptr);
+        }
+        b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
+        set_error(b.status, err);
+    }
+}
+
+// Blocks of at most 256 threads. kThreadsPerSm > 0 caps registers so that many threads fit on
+// an SM (512: 128 registers, no spills; 768: 85 registers, a few spills); 0 leaves the
+// compiler's choice.
+template <bool kOne, int kThreadsPerSm>
+__global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
+    engine_shade_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    __shared__ int smem[33];
+    EngineCtl* ctl = b.ctl;
+    const int n = ctl->count[parity];
+    const int* qin = b.queue[parity];
+    int* qout = b.queue[parity ^ 1];
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)   // block-uniform
+    {
+        const int i = base + threadIdx.x;
+        bool pushExt = false, pushShadow = false, finished = false;
+        int p = -1;
+        ShadowRec rec;
+        if (i < n)
+        {
+            p = qin[i];
+            if constexpr (kOne)
+                shade_path(one.S, one.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
+            else
+            {
+                const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
+                const EngineJob& J = b.jobs[job_of(w)];
+                shade_path(J.S, J.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
+            }
+            finished = !pushExt;
+        }
+        block_push(pushExt, p, qout, &ctl->count[parity ^ 1], b.cap, b.status, smem);
+        block_push(pushShadow, rec, b.shadow, &ctl->shadowCount, b.cap, b.status, smem);
+        block_push(finished, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
+    }
+}
+
+template <bool kOne>
+__global__ void engine_shadow_kernel(EngineBuffers b, EngineJob one)
+{
+    const int n = b.ctl->shadowCount;
+    unsigned long long rays = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const ShadowRec rec = b.shadow[i];
+        if constexpr (kOne)
+            set_error(b.status, shadow_path(one.S, one.P, b.ps, rec, rays));
+        else
+        {
+            const int p = __float_as_int(rec.a.w);
+            const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
+            const EngineJob& J = b.jobs[job_of(w)];
+            set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, rays));
+        }
+    }
+    warp_count_add(&b.ctr[2], rays);
+}
+
+// ------------------------------------------------------------------ accumulate
+__global__ void engine_accumulate_kernel(int width, int tileW, int tileH, EnginePass Q, float4* accum, double* accum64)
+{
+    const int visPix = Q.visW * Q.visH;
+    for (int lp = blockIdx.x * blockDim.x + threadIdx.x; lp < visPix; lp += gridDim.x * blockDim.x)
+    {
+        const int lx = lp % Q.visW, ly = lp / Q.visW;
+        const int gpix = (Q.tileY * tileH + ly) * width + Q.tileX * tileW + lx;
+        float4 a = accum[gpix];
+        double ax = 0, ay = 0, az = 0;
+        if (accum64)
+        {
+            ax = accum64[gpix * 3 + 0];
+            ay = accum64[gpix * 3 + 1];
+            az = accum64[gpix * 3 + 2];
+        }
+        for (int s = 0; s < Q.nSamples; ++s)
+        {
+            const float4 l = Q.radiance[(size_t)s * visPix + lp];
+            a.x = a.x + l.x;
+            a.y = a.y + l.y;
+            a.z = a.z + l.z;
+            if (accum64)
+            {
+                ax += (double)l.x;
+                ay += (double)l.y;
+                az += (double)l.z;
+            }
+        }
+        accum[gpix] = a;
+        if (accum64)
+        {
+            accum64[gpix * 3 + 0] = ax;
+            accum64[gpix * 3 + 1] = ay;
+            accum64[gpix * 3 + 2] = az;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+namespace
+{
+int sm_count()
+{
+    static int n = 0;
+    if (n == 0)
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+int full_grid(const void* kernel, int block, long long work)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (per_sm <= 0) per_sm = 1;
+    long long full = (long long)sm_count() * per_sm;
+    long long need = (work + block - 1) / block;
+    if (need < 1) need = 1;
+    return (int)(need < full ? need : full);
+}
+}
+
+int launch_engine_init(const EngineBuffers& b, cudaStream_t st)
+{
+    engine_init_kernel<<<full_grid((const void*)engine_init_kernel, 256, b.cap), 256, 0, st>>>(b);
+    return (int)cudaGetLastError();
+}
+
+int launch_engine_append(const EngineBuffers& b, unsigned long long total, unsigned long long numPasses,
+                         cudaStream_t st)
+{
+    engine_append_kernel<<<1, 1, 0, st>>>(b, total, numPasses);
+    return (int)cudaGetLastError();
+}
+
+namespace
+{
+template <bool kOne>
+void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t st)
+{
+    const int BF = 256;
+    engine_finish_kernel<kOne><<<full_grid((const void*)engine_finish_kernel<kOne>, BF, b.cap), BF, 0, st>>>(b, one,
+                                                                                                          parity);
+    engine_reset_kernel<<<1, 1, 0, st>>>(b.ctl, parity);
+    const int be = b.blockExtend > 0 ? b.blockExtend : 128;
+    const int bs = b.blockShade > 0 ? b.blockShade : 128;
+    const int bw = b.blockShadow > 0 ? b.blockShadow : 128;
+    engine_extend_kernel<kOne><<<full_grid((const void*)engine_extend_kernel<kOne>, be, b.cap), be, 0, st>>>(b, one,
+                                                                                                           parity);
+    if (b.shadeThreadsPerSm == 512)
+        engine_shade_kernel<kOne, 512><<<full_grid((const void*)engine_shade_kernel<kOne, 512>, bs, b.cap), bs, 0, st>>>(
+            b, one, parity);
+    else if (b.shadeThreadsPerSm == 768)
+        engine_shade_kernel<kOne, 768><<<full_grid((const void*)engine_shade_kernel<kOne, 768>, bs, b.cap), bs, 0, st>>>(
+            b, one, parity);
+    else
+        engine_shade_kernel<kOne, 0><<<full_grid((const void*)engine_shade_kernel<kOne, 0>, bs, b.cap), bs, 0, st>>>(
+            b, one, parity);
+    engine_shadow_kernel<kOne><<<full_grid((const void*)engine_shadow_kernel<kOne>, bw, b.cap), bw, 0, st>>>(b, one);
+}
+}
+
+int launch_engine_step(const EngineBuffers& b, const EngineJob* one, int parity, cudaStream_t st)
+{
+    if (one)
+        step<true>(b, *one, parity, st);
+    else
+        step<false>(b, EngineJob{}, parity, st);
+    return (int)cudaGetLastError();
+}
+
+int launch_engine_accumulate(const Params& P, const EnginePass& pass, float4* accum, double* accum64,
+                             cudaStream_t st)
+{
+    const int B = 256;
+    const long long pix = (long long)pass.visW * pass.visH;
+    engine_accumulate_kernel<<<full_grid((const void*)engine_accumulate_kernel, B, pix), B, 0, st>>>(
+        P.width, P.tileW, P.tileH, pass, accum, accum64);
+    return (int)cudaGetLastError();
+}
+}

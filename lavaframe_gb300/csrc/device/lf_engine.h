@@ -1,0 +1,88 @@
+// Persistent multi-job wavefront engine: device-side tables and launch interface
+// (kernels in lf_engine.cu, host driver in lf_engine_host.cu).
+//
+// A fixed pool of path slots runs paths of many render passes at once. A pass is a range of
+// samples of one tile of one job; its paths get consecutive global ids, and a slot whose path
+// finished immediately starts the next unissued id (path regeneration), so the extension and
+// shadow queues stay full until the work runs out instead of shrinking bounce by bounce.
+// Each path writes its radiance into its pass's buffer ([sample][pixel of the visible tile])
+// and the pass is accumulated per pixel in sample order once all its paths are done, so the
+// image sums are the ones of the per-batch pipeline, bit for bit.
+//
+// One engine step with parity k (graph-captured, two steps per graph so the parity returns):
+//   finish   done[k]: write out finished paths, count pass completions, start new paths
+//            (-> queue[k]); slots left without work go to done[k^1]
+//   reset    clear done[k], the shadow queue and queue[k^1]
+//   extend   closest hit of every queued path
+//   shade    one PathTrace bounce; survivors -> queue[k^1], finished -> done[k^1]
+//   shadow   next-event visibility
+#pragma once
+
+#include "lf_kernels.h"
+
+namespace lfd
+{
+constexpr int kPassRingBits = 14;
+constexpr int kPassRing = 1 << kPassRingBits;   // pass descriptors in flight
+constexpr int kMaxEngineJobs = 1 << 16;         // job slots (packed into the upper bits of info.w)
+
+struct EngineJob
+{
+    ShadeScene S;   // environment multiplier already applied
+    Params P;       // job-level parameters; tile fields describe the tile size only
+};
+
+struct EnginePass
+{
+    int job;                     // job slot
+    int firstSample, nSamples;
+    int tileX, tileY, tileOrdinal;
+    int visW, visH;              // visible part of the tile
+    unsigned long long pathBase; // global id of the first path
+    unsigned long long numPaths; // nSamples * visW * visH
+    float4* radiance;            // numPaths entries, [sample][visible pixel]
+};
+
+struct EngineCtl
+{
+    unsigned long long next;       // next global path id to issue (may overshoot total)
+    unsigned long long total;      // ids available
+    unsigned long long passLo;     // first pass that may still have unissued ids
+    unsigned long long numPasses;  // passes submitted
+    int count[2];                  // extension queue sizes
+    int shadowCount;
+    int doneCount[2];              // done-list sizes
+    int active;                    // paths started and not yet written out
+};
+
+struct EngineBuffers
+{
+    PathSoA ps;                  // info: x local path id, y depth, z last material, w ring | job << 14
+    int* queue[2];
+    ShadowRec* shadow;
+    int* done[2];                // slots whose path finished, or that are idle
+    EngineCtl* ctl;
+    const EngineJob* jobs;
+    const EnginePass* passes;    // ring of kPassRing
+    unsigned long long* passDone;// completed paths per ring entry
+    uint32_t* status;
+    unsigned long long* ctr;     // [1] extension rays, [2] shadow rays, [3] light-index clamps
+    int cap;                     // pool slots
+    int blockExtend, blockShade, blockShadow;
+    int shadeThreadsPerSm;       // register cap of the shade kernel: 0 none, 512 or 768
+};
+
+// Launches one engine step with queue parity `parity` on `st`. With `one` set, every path
+// belongs to that job and the kernels read it from their parameters (constant bank) instead
+// of the job table.
+int launch_engine_step(const EngineBuffers& b, const EngineJob* one, int parity, cudaStream_t st);
+// Pool start: every slot on the done list, marked unused.
+int launch_engine_init(const EngineBuffers& b, cudaStream_t st);
+// Publishes newly written pass descriptors: clamps the overshoot of `next` to the old total,
+// then raises total / numPasses and advances passLo past fully issued passes.
+int launch_engine_append(const EngineBuffers& b, unsigned long long total, unsigned long long numPasses,
+                         cudaStream_t st);
+// Per-pixel in-order sum of one completed pass into the job's accumulation buffers.
+int launch_engine_accumulate(const Params& P, const EnginePass& pass, float4* accum, double* accum64,
+                             cudaStream_t st);
+}

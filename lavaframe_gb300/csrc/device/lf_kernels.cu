@@ -10,47 +10,12 @@
 // Path state lives in SoA arrays in HBM; queues are compacted with one atomic per warp
 // (ballot + popc). Every kernel runs a warp-uniform grid-stride loop over a device-side
 // count, so the bounce loop needs no host round trip and can be captured in a graph.
-#include "lf_kernels.h"
-#include "lf_shade.cuh"
+#include "lf_pathops.cuh"
 
 namespace lfd
 {
-namespace
-{
-constexpr unsigned kFull = 0xffffffffu;
+using namespace pathops;
 
-__device__ __forceinline__ void set_error(uint32_t* status, uint32_t bits)
-{
-    if (bits && status) atomicOr(status, bits);
-}
-
-// Appends `item` for lanes with `pred`; one atomic per warp. All 32 lanes must call.
-template <class T>
-__device__ __forceinline__ void warp_push(bool pred, const T& item, T* queue, int* count, int cap, uint32_t* status)
-{
-    unsigned m = __ballot_sync(kFull, pred);
-    if (!m) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(count, __popc(m));
-    base = __shfl_sync(kFull, base, leader);
-    if (pred)
-    {
-        int pos = base + __popc(m & ((1u << lane) - 1u));
-        if (pos < cap) queue[pos] = item;
-        else set_error(status, LF_DEVERR_QUEUE);
-    }
-}
-
-__device__ __forceinline__ v3 f3(float4 a) { return v3(a.x, a.y, a.z); }
-__device__ __forceinline__ float4 f4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
-
-__device__ __forceinline__ float map_range(float value, float low1, float high1, float low2, float high2)
-{
-    return low2 + ((value - low1) * (high2 - low2)) / (high1 - low1);
-}
-}
 
 // ------------------------------------------------------------------ generate
 __global__ void generate_kernel(ShadeScene S, Params P, PathSoA ps, int firstSample, int nSamples, int* queue,
@@ -77,54 +42,7 @@ __global__ void generate_kernel(ShadeScene S, Params P, PathSoA ps, int firstSam
             ps.info[slot] = make_int4(inside ? gy * P.width + gx : -1, 0, 0, 0);
             if (inside)
             {
-                // renderer.glsl:27-62
-                float tcx = ((float)lx + 0.5f) / (float)P.tileW;
-                float tcy = ((float)ly + 0.5f) / (float)P.tileH;
-                float xoffset = -1.0f + 2.0f * P.invNumTilesX * (float)P.tileX;
-                float yoffset = -1.0f + 2.0f * P.invNumTilesY * (float)P.tileY;
-                float ctx = map_range(tcx, 0.0f, 1.0f, xoffset, xoffset + 2.0f * P.invNumTilesX);
-                float cty = map_range(tcy, 0.0f, 1.0f, yoffset, yoffset + 2.0f * P.invNumTilesY);
-                float fsx = map_range(tcx, 0.0f, 1.0f, P.invNumTilesX * (float)P.tileX,
-                                      P.invNumTilesX * (float)P.tileX + P.invNumTilesX);
-                float fsy = map_range(tcy, 0.0f, 1.0f, P.invNumTilesY * (float)P.tileY,
-                                      P.invNumTilesY * (float)P.tileY + P.invNumTilesY);
-                float px = fsx * (float)P.width, py = fsy * (float)P.height;
-                uint32_t frame = (uint32_t)(P.frameBase + (firstSample + s) * P.frameStride + P.tileOrdinal);
-                Rng rng;
-                rng.x = (uint32_t)px;
-                rng.y = (uint32_t)py;
-                rng.z = frame;
-                rng.w = (uint32_t)px + (uint32_t)py + P.seed * 0x9E3779B9u;
-
-                float r1 = 2.0f * rnd(rng);
-                float r2 = 2.0f * rnd(rng);
-                float jx = r1 < 1.0f ? sqrtf(r1) - 1.0f : 1.0f - sqrtf(2.0f - r1);
-                float jy = r2 < 1.0f ? sqrtf(r2) - 1.0f : 1.0f - sqrtf(2.0f - r2);
-                jx = jx / ((float)P.width * 0.5f);
-                jy = jy / ((float)P.height * 0.5f);
-                float dx = ctx + jx, dy = cty + jy;
-                float scale = lfc::tan_c(P.fov * 0.5f);
-                dy = dy * ((float)P.height / (float)P.width * scale);
-                dx = dx * scale;
-                v3 right(P.cam_right[0], P.cam_right[1], P.cam_right[2]);
-                v3 up(P.cam_up[0], P.cam_up[1], P.cam_up[2]);
-                v3 fwd(P.cam_fwd[0], P.cam_fwd[1], P.cam_fwd[2]);
-                v3 rayDir = lfc::normalize(dx * right + dy * up + fwd);
-                v3 focalPoint = P.focalDist * rayDir;
-                float cam_r1 = rnd(rng) * kTWO_PI;
-                float cam_r2 = rnd(rng) * P.aperture;
-                float sr, cr;
-                lfc::sincos_c(cam_r1, &sr, &cr);
-                v3 aperturePos = (cr * right + sr * up) * sqrtf(cam_r2);
-                v3 dir = lfc::normalize(focalPoint - aperturePos);
-                v3 org = v3(P.cam_pos[0], P.cam_pos[1], P.cam_pos[2]) + aperturePos;
-
-                ps.o[slot] = f4(org, 0.0f);
-                ps.d[slot] = f4(dir, 0.0f);
-                ps.T[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-                ps.A[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-                ps.rng[slot] = make_uint4(rng.x, rng.y, rng.z, rng.w);
-                ps.luv[slot] = make_float2(0.f, 0.f);
+                gen_path(P, P.tileX, P.tileY, P.tileOrdinal, firstSample + s, lx, ly, ps, slot);
                 push = true;
             }
         }
@@ -151,9 +69,11 @@ __global__ void extend_kernel(ShadeScene S, Params P, PathSoA ps, const int* que
 }
 
 // ------------------------------------------------------------------ shade
-__global__ void shade_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin, const int* qinCount, int* qout,
-                             int* qoutCount, ShadowRec* sq, int* sqCount, int cap, uint32_t* status,
-                             unsigned long long* ctr)
+// 4 blocks of 128 threads per SM: caps registers at 128 (no spills).
+__global__ void __launch_bounds__(128, 4) shade_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin,
+                                                        const int* qinCount, int* qout, int* qoutCount, ShadowRec* sq,
+                                                        int* sqCount, int cap, uint32_t* status,
+                                                        unsigned long long* ctr)
 {
     const int n = *qinCount;
     const int stride = gridDim.x * blockDim.x;
@@ -168,211 +88,7 @@ __global__ void shade_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin,
         if (i < n)
         {
             p = qin[i];
-            float4 o4 = ps.o[p], d4 = ps.d[p], T4 = ps.T[p], L4 = ps.L[p], A4 = ps.A[p], h = ps.hit[p];
-            int4 info = ps.info[p];
-            uint4 r4 = ps.rng[p];
-            Rng rng{r4.x, r4.y, r4.z, r4.w};
-            v3 o = f3(o4), d = f3(d4), T = f3(T4), L = f3(L4), A = f3(A4);
-            float bsdfPdf = o4.w;
-            const int depth = info.y;
-            const float t = h.x;
-            const int inst = __float_as_int(h.y), prim = __float_as_int(h.z), light = __float_as_int(h.w);
-
-            if (t == kInfinity)
-            {
-                if (P.constantBg)
-                    L = L + v3(P.bg[0], P.bg[1], P.bg[2]) * T;
-                else if (P.envOnMiss)
-                {
-                    float mis = 1.0f;
-                    v3 col = env_lookup(S.env, d);
-                    if (depth > 0)
-                    {
-                        float lightPdf = EnvPdf(S.env, d);
-                        mis = powerHeuristic(bsdfPdf, lightPdf);
-                    }
-                    L = L + mis * col * T * S.env.multiplier;
-                }
-                ps.L[p] = f4(L, 0.f);
-            }
-            else if (light >= 0)
-            {
-                // Analytic light: the shader still adds the emission of the material held
-                // in the (stale) state from the last triangle hit before EmitterSample.
-                v3 em = material_emission(S, info.z, lfc::v2(ps.luv[p].x, ps.luv[p].y));
-                L = L + em * T;
-                const DevLight& Lt = S.trav.lights[light];
-                v3 Le(Lt.emission[0], Lt.emission[1], Lt.emission[2]);
-                if (depth != 0)
-                {
-                    float lpdf;
-                    if (Lt.type == 0.f)
-                    {
-                        float cosTheta = lfc::dot(-d, v3(Lt.normal[0], Lt.normal[1], Lt.normal[2]));
-                        lpdf = (t * t) / (Lt.area * cosTheta);
-                    }
-                    else
-                        lpdf = (t * t) / Lt.area;
-                    Le = powerHeuristic(bsdfPdf, lpdf) * Le;
-                }
-                L = L + Le * T;
-                ps.L[p] = f4(L, 0.f);
-            }
-            else
-            {
-                // ---- GetNormalsAndTexCoord (pathtrace.glsl:16-37)
-                float m[12];
-                int root, matId;
-                load_instance(S.trav.instances + (size_t)inst * 4, m, &root, &matId);
-                const ShadeInstance& SI = S.inst[inst];
-                v3 ro = xform(m, o, 1.0f), rd = xform(m, d, 0.0f);
-                float u, v;
-                tri_hit(S.trav.tris + (size_t)prim * 3, ro, rd, &u, &v);
-                float bw = 1.0f - u - v;
-                v3 fhp = xform(SI.fwd, ro + rd * t, 1.0f);
-                int4 vi = S.vertIndices[prim];
-                float4 n1 = S.normals[vi.x], n2 = S.normals[vi.y], n3 = S.normals[vi.z];
-                float w0 = S.vertices[vi.x].w, w1 = S.vertices[vi.y].w, w2 = S.vertices[vi.z].w;
-                Surf s;
-                s.texCoord = lfc::v2(w0, n1.w) * bw + lfc::v2(w1, n2.w) * u + lfc::v2(w2, n3.w) * v;
-                v3 nrm = lfc::normalize(f3(n1) * bw + f3(n2) * u + f3(n3) * v);
-                nrm = lfc::normalize(lfc::mul3(SI.nrm, nrm));
-                s.normal = nrm;
-                s.ffnormal = lfc::dot(nrm, d) <= 0.0f ? nrm : nrm * -1.0f;
-                Onb(s.normal, s.tangent, s.bitangent);
-                // ---- GetMaterialsAndTextures (pathtrace.glsl:40-123)
-                s.mat = load_material(S, SI.material);
-                apply_textures(S, s, d);
-                s.eta = lfc::dot(d, s.normal) < 0.0f ? (1.0f / s.mat.ior) : s.mat.ior;
-                info.z = SI.material;
-                ps.luv[p] = make_float2(s.texCoord.x, s.texCoord.y);
-
-                if (lfc::dot(s.normal, s.ffnormal) > 0.0f) A = v3(0.0f);
-                L = L + s.mat.emission * T;
-                T = T * lfc::vexp(-A * t);
-
-                // ---- DirectLight (pathtrace.glsl:126-204): candidates, visibility later
-                BsdfCtx bc{s.eta, s.mat, s.tangent, s.bitangent};
-                v3 V = -d;
-                v3 surfacePos = fhp + s.normal * kEps;
-                uint32_t flags = 0;
-                v3 envDir(0.f), envC(0.f), lightDir(0.f), lightC(0.f);
-                float lightMax = 0.f;
-                if (P.useEnv)
-                {
-                    v3 color;
-                    float4 dp = EnvSample(S.env, rng, color);
-                    envDir = v3(dp.x, dp.y, dp.z);
-                    float lightPdf = dp.w;
-                    float pdf;
-                    v3 f = DisneyEval(bc, V, s.ffnormal, envDir, pdf);
-                    if (pdf > 0.0f)
-                    {
-                        float mis = powerHeuristic(lightPdf, pdf);
-                        if (mis > 0.0f)
-                        {
-                            envC = mis * f * fabsf(lfc::dot(envDir, s.ffnormal)) * color / lightPdf;
-                            flags |= 1u;
-                        }
-                    }
-                }
-                if (P.useLights)
-                {
-                    const int nl = S.trav.numLights;
-                    int li = (int)(rnd(rng) * (float)nl);
-                    if (li >= nl)
-                    {
-                        li = nl - 1;
-                        atomicAdd(&ctr[3], 1ull);
-                    }
-                    const DevLight& Lt = S.trav.lights[li];
-                    v3 lpos(Lt.pos[0], Lt.pos[1], Lt.pos[2]);
-                    v3 ldir, lnrm;
-                    float ldist, lpdf;
-                    v3 lem = v3(Lt.emission[0], Lt.emission[1], Lt.emission[2]) * (float)nl;
-                    int type = (int)Lt.type;
-                    if (type == 0 || type == 1)
-                    {
-                        float r1 = rnd(rng);
-                        float r2 = rnd(rng);
-                        v3 lsp;
-                        if (type == 0)
-                            lsp = lpos + v3(Lt.u[0], Lt.u[1], Lt.u[2]) * r1 + v3(Lt.v[0], Lt.v[1], Lt.v[2]) * r2;
-                        else
-                            lsp = lpos + UniformSampleSphere(r1, r2) * Lt.radius;
-                        ldir = lsp - surfacePos;
-                        ldist = lfc::length(ldir);
-                        float distSq = ldist * ldist;
-                        ldir = ldir / ldist;
-                        lnrm = type == 0 ? v3(Lt.normal[0], Lt.normal[1], Lt.normal[2]) : lfc::normalize(lsp - lpos);
-                        lpdf = distSq / (Lt.area * fabsf(lfc::dot(lnrm, ldir)));
-                    }
-                    else
-                    {
-                        ldir = lfc::normalize(lpos - v3(0.0f));
-                        lnrm = lfc::normalize(surfacePos - lpos);
-                        ldist = kInfinity;
-                        lpdf = 1.0f;
-                    }
-                    if (lfc::dot(ldir, lnrm) < 0.0f)
-                    {
-                        float pdf;
-                        v3 f = DisneyEval(bc, V, s.ffnormal, ldir, pdf);
-                        float weight = 1.0f;
-                        if (Lt.area > 0.0f) weight = powerHeuristic(lpdf, pdf);
-                        if (pdf > 0.0f)
-                        {
-                            lightC = weight * f * fabsf(lfc::dot(s.ffnormal, ldir)) * lem / lpdf;
-                            lightDir = ldir;
-                            lightMax = ldist - kEps;
-                            flags |= 2u;
-                        }
-                    }
-                }
-                if (flags)
-                {
-                    rec.a = f4(surfacePos, __int_as_float(p));
-                    rec.b = f4(T, __uint_as_float(flags));
-                    rec.c = f4(envDir, 0.f);
-                    rec.e = f4(envC, 0.f);
-                    rec.f = f4(lightDir, lightMax);
-                    rec.g = f4(lightC, 0.f);
-                    pushShadow = true;
-                }
-                else
-                    L = L + v3(0.0f) * T;
-
-                // ---- DisneySample, absorption, throughput, RR (pathtrace.glsl:268-291)
-                v3 Ls;
-                float pdf;
-                v3 f = DisneySample(bc, rng, V, s.ffnormal, Ls, pdf);
-                if (lfc::dot(s.ffnormal, Ls) < 0.0f) A = (-lfc::vlog(s.mat.extinction)) / s.mat.atDistance;
-                bool alive = true;
-                if (pdf > 0.0f)
-                    T = T * (f * fabsf(lfc::dot(s.ffnormal, Ls)) / pdf);
-                else
-                    alive = false;
-                if (alive && P.rrEnabled && depth >= P.rrDepth)
-                {
-                    float q = lfc::fmin_g(lfc::fmax_g(T.x, lfc::fmax_g(T.y, T.z)) + 0.001f, 0.95f);
-                    if (rnd(rng) > q) alive = false;
-                    else T = T / q;
-                }
-                if (alive)
-                {
-                    d = Ls;
-                    o = fhp + d * kEps;
-                    if (depth + 1 < P.maxDepth) pushExt = true;
-                }
-                info.y = depth + 1;
-                ps.o[p] = f4(o, pdf);
-                ps.d[p] = f4(d, 0.f);
-                ps.T[p] = f4(T, 0.f);
-                ps.L[p] = f4(L, 0.f);
-                ps.A[p] = f4(A, 0.f);
-                ps.rng[p] = make_uint4(rng.x, rng.y, rng.z, rng.w);
-                ps.info[p] = info;
-            }
+            shade_path(S, P, ps, p, ctr, pushExt, pushShadow, rec);
         }
         warp_push(pushExt, p, qout, qoutCount, cap, status);
         warp_push(pushShadow, rec, sq, sqCount, cap, status);
@@ -384,36 +100,10 @@ __global__ void shadow_kernel(ShadeScene S, Params P, PathSoA ps, const ShadowRe
                               uint32_t* status, unsigned long long* ctr)
 {
     const int n = *sqCount;
-    const bool lights = P.useLights != 0;
     unsigned long long rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        ShadowRec rec = sq[i];
-        int p = __float_as_int(rec.a.w);
-        uint32_t flags = __float_as_uint(rec.b.w);
-        v3 pos = f3(rec.a);
-        v3 Li(0.0f);
-        Hit h;
-        bool occ;
-        uint32_t err = 0;
-        if (flags & 1u)
-        {
-            err |= any_hit<false>(S.trav, pos, f3(rec.c), kInfinity - kEps, lights, &occ, &h, nullptr);
-            if (!occ) Li = Li + f3(rec.e);
-            ++rays;
-        }
-        if (flags & 2u)
-        {
-            err |= any_hit<false>(S.trav, pos, f3(rec.f), rec.f.w, lights, &occ, &h, nullptr);
-            if (!occ) Li = Li + f3(rec.g);
-            ++rays;
-        }
-        float4 L4 = ps.L[p];
-        v3 L = f3(L4) + Li * f3(rec.b);
-        ps.L[p] = f4(L, 0.f);
-        set_error(status, err);
-    }
-    if (rays) atomicAdd(&ctr[2], rays);
+        set_error(status, shadow_path(S, P, ps, sq[i], rays));
+    warp_count_add(&ctr[2], rays);
 }
 
 // ------------------------------------------------------------------ persistent extend / shadow
@@ -532,7 +222,7 @@ __global__ void __launch_bounds__(128) shadow_persistent_kernel(ShadeScene S, Pa
             ++phase;
         }
     }
-    if (rays) atomicAdd(&ctr[2], rays);
+    warp_count_add(&ctr[2], rays);
 }
 
 // ------------------------------------------------------------------ accumulate

@@ -10,135 +10,9 @@
 #include <string>
 #include <vector>
 
-#include "../../../include/lavaframe_gb300.h"
-#include "lf_kernels.h"
+#include "lf_engine_host.h"
 
-using namespace lfd;
-
-struct lf_ctx
-{
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::recursive_mutex mu;
-    std::string err;
-    uint32_t* d_status = nullptr;
-    unsigned long long* d_stats = nullptr;   // [3] traversal counters
-    uint32_t devErrors = 0;
-    uint64_t lastStats[3] = {0, 0, 0};
-    // reusable device buffers of the host-pointer ray queries
-    void* scratchRays = nullptr;
-    size_t scratchRaysBytes = 0;
-    void* scratchOut = nullptr;
-    size_t scratchOutBytes = 0;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    // scratch of the binned ray queries
-    uint32_t* binKeys = nullptr;
-    int* binPerm = nullptr;
-    size_t binCap = 0;
-    uint32_t* binHist = nullptr;
-    unsigned long long* binNext = nullptr;
-};
-
-struct lf_scene
-{
-    lf_ctx* ctx = nullptr;
-    std::vector<void*> allocs;
-    size_t bytes = 0;
-    ShadeScene view{};
-    // re-encoding metadata for instance updates
-    int numRefNodes = 0;
-    int topLevelIndex = 0;
-    int numMeshNodes = 0;       // device records that belong to mesh levels
-    std::vector<int> blasRootCode;   // per reference node index of a mesh root (code), lazily
-    float4* d_nodes = nullptr;
-    size_t nodeCapacity = 0;    // records allocated
-    float4* d_instances = nullptr;
-    ShadeInstance* d_sinst = nullptr;
-    DevMaterial* d_materials = nullptr;
-    int numMaterials = 0;
-    std::vector<int> meshNodeMap;   // reference index -> device record (mesh levels), -1 otherwise
-    float boundsLo[3] = {0, 0, 0}, boundsHi[3] = {0, 0, 0};   // instance-level root box
-};
-
-struct lf_frame
-{
-    lf_ctx* ctx = nullptr;
-    lf_scene* scene = nullptr;
-    Params P{};
-    uint32_t flags = 0;
-    int W = 0, H = 0;
-    int numTilesX = 1, numTilesY = 1;
-    int sppBatch = 0;
-    long long cap = 0;   // path slots
-    float4* accum = nullptr;
-    double* accum64 = nullptr;
-    PathSoA ps{};
-    BounceBuffers bb{};
-    std::vector<void*> fixedAllocs;   // accumulation buffers and counters
-    std::vector<void*> allocs;        // path state and queues (sized by the batch)
-    uint64_t paths = 0;
-    int lastBatchSamples = 0;
-    cudaGraphExec_t graph = nullptr;
-    int graphDepth = -1;
-};
-
-namespace
-{
-lf_status fail(lf_ctx* c, lf_status st, const std::string& msg)
-{
-    if (c) c->err = msg;
-    return st;
-}
-
-lf_status cuda_fail(lf_ctx* c, cudaError_t e, const char* what)
-{
-    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-    if (e == cudaErrorMemoryAllocation) return fail(c, LF_ERR_OOM, m);
-    return fail(c, LF_ERR_CUDA, m);
-}
-
-template <class T>
-cudaError_t dalloc(std::vector<void*>& list, size_t& bytes, T** p, size_t count)
-{
-    *p = nullptr;
-    if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
-    if (e == cudaSuccess)
-    {
-        list.push_back(*p);
-        bytes += sizeof(T) * count;
-    }
-    return e;
-}
-
-lf_status check_device(lf_ctx* c)
-{
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronize");
-    uint32_t bits = 0;
-    e = cudaMemcpy(&bits, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
-    if (bits)
-    {
-        c->devErrors |= bits;
-        cudaMemset(c->d_status, 0, sizeof(uint32_t));
-        return fail(c, LF_ERR_DEVICE, "device error bits 0x" + std::to_string(bits));
-    }
-    return LF_OK;
-}
-
-struct RefNode
-{
-    float bmin[3], bmax[3], lr[3];
-};
-
-float ulp_of(float x)
-{
-    x = std::fabs(x);
-    float n = std::nextafter(x, INFINITY);
-    return n - x;
-}
-}
+using namespace lfrt;
 
 extern "C" {
 
@@ -170,6 +44,8 @@ void lf_ctx_destroy(lf_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    engine_destroy(c->engine);
+    c->engine = nullptr;
     cudaFree(c->d_status);
     cudaFree(c->d_stats);
     cudaFree(c->scratchRays);
@@ -917,7 +793,8 @@ lf_status lf_frame_create(lf_ctx* c, lf_scene* sc, const lf_render_params* p, ui
     if (e == cudaSuccess) e = dalloc(f->fixedAllocs, bytes, &ctr, 4);
     f->bb.ctr = ctr;
     f->bb.status = c->d_status;
-    lf_status st = e == cudaSuccess ? alloc_paths(f, (long long)f->sppBatch * tilePix) : cuda_fail(c, e, "frame allocation");
+    // per-batch path state is allocated on first use (the engine has its own pool)
+    lf_status st = e == cudaSuccess ? LF_OK : cuda_fail(c, e, "frame allocation");
     if (st != LF_OK)
     {
         for (void* q : f->fixedAllocs) cudaFree(q);
@@ -941,19 +818,47 @@ lf_status lf_frame_set_batch(lf_frame* f, int32_t spb)
     int want = spb == 0 ? (int)std::max(1LL, std::min(64LL, (8LL << 20) / tilePix)) : spb;
     if (want == f->sppBatch) return LF_OK;
     cudaStreamSynchronize(c->stream);
-    free_frame_buffers(f);
+    free_frame_buffers(f);   // per-batch state is reallocated at the next batch
     if (f->graph)
     {
         cudaGraphExecDestroy(f->graph);
         f->graph = nullptr;
     }
     f->sppBatch = want;
-    lf_status st = alloc_paths(f, (long long)want * tilePix);
-    return st;
+    return LF_OK;
 }
 
 namespace
 {
+// Ends the capture begun by run_batch, updates (or instantiates) the frame's graph with the
+// recorded batch and launches it.
+lf_status end_batch_graph(lf_frame* f, cudaError_t launchErr, const char* what)
+{
+    lf_ctx* c = f->ctx;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (launchErr != cudaSuccess || e != cudaSuccess)
+    {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(c, launchErr != cudaSuccess ? launchErr : e, what);
+    }
+    if (f->graph)
+    {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(f->graph, g, &info) != cudaSuccess)
+        {
+            cudaGetLastError();
+            cudaGraphExecDestroy(f->graph);
+            f->graph = nullptr;
+        }
+    }
+    if (!f->graph) e = cudaGraphInstantiate(&f->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e == cudaSuccess) e = cudaGraphLaunch(f->graph, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "batch graph launch");
+    return LF_OK;
+}
+
 // One batch of samples on one tile: generate, maxDepth bounces, accumulate.
 lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
 {
@@ -963,23 +868,33 @@ lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
     Sv.env.multiplier = P.hdrMultiplier;
     long long tilePix = (long long)P.tileW * P.tileH;
     long long cap = (long long)n * tilePix;
+    if (f->cap < cap)
+    {
+        free_frame_buffers(f);
+        lf_status st = alloc_paths(f, (long long)std::max(n, f->sppBatch) * tilePix);
+        if (st != LF_OK) return st;
+    }
+    const bool graph = (f->flags & LF_FRAME_USE_GRAPH) != 0;
+    if (graph)
+    {
+        cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+        if (ce != cudaSuccess) return cuda_fail(c, ce, "batch graph capture");
+    }
     cudaMemsetAsync(f->bb.count, 0, 2 * sizeof(int), c->stream);
     int e = launch_generate(Sv, P, f->ps, firstSample, n, f->bb.queue[0], f->bb.count, c->stream);
-    if (e) return cuda_fail(c, (cudaError_t)e, "generate launch");
+    if (e) return graph ? end_batch_graph(f, cudaErrorLaunchFailure, "generate launch")
+                        : cuda_fail(c, (cudaError_t)e, "generate launch");
     BounceBuffers bb = f->bb;
     // Queue order is already coherent (camera rays in pixel order, survivors compacted in
     // order), and one thread per queued ray measured faster than persistent warps on the
     // icosphere scenes; LF_WAVEFRONT_PERSISTENT=1 selects the persistent extend/shadow kernels.
     static const bool persistent = std::getenv("LF_WAVEFRONT_PERSISTENT") != nullptr;
     if (!persistent) bb.fetch = nullptr;
-    for (int b = 0; b < P.maxDepth; ++b)
-    {
-        e = launch_bounce(Sv, P, f->ps, bb, b, cap, c->stream);
-        if (e) return cuda_fail(c, (cudaError_t)e, "bounce launch");
-    }
-    e = launch_accumulate(P, f->ps, n, f->accum, f->accum64, c->stream);
-    if (e) return cuda_fail(c, (cudaError_t)e, "accumulate launch");
+    for (int b = 0; b < P.maxDepth && !e; ++b) e = launch_bounce(Sv, P, f->ps, bb, b, cap, c->stream);
+    if (!e) e = launch_accumulate(P, f->ps, n, f->accum, f->accum64, c->stream);
     f->lastBatchSamples = n;
+    if (graph) return end_batch_graph(f, (cudaError_t)e, "batch launch");
+    if (e) return cuda_fail(c, (cudaError_t)e, "batch launch");
     return LF_OK;
 }
 }
@@ -993,6 +908,19 @@ lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count)
     Params P = f->P;
     const bool tiledFrames = (f->flags & LF_FRAME_TILED_FRAMES) != 0;
     P.frameStride = tiledFrames ? f->numTilesX * f->numTilesY : 1;
+    if (!(f->flags & LF_FRAME_PER_BATCH))
+    {
+        if (count == 0) return LF_OK;
+        lf_status st = frame_render_engine(f, P, first_sample, count);
+        if (st == LF_OK) f->paths += (uint64_t)count * f->W * f->H;
+        return st;
+    }
+    if (f->lastRadiance)
+    {
+        cudaFreeAsync(f->lastRadiance, c->stream);
+        f->lastRadiance = nullptr;
+        f->lastRadianceSamples = 0;
+    }
     int s = 0;
     while (s < count)
     {
@@ -1025,6 +953,12 @@ lf_status lf_frame_render_tile(lf_frame* f, int32_t sample, int32_t tile_x, int3
     P.tileX = tile_x;
     P.tileY = tile_y;
     P.tileOrdinal = tiledFrames ? (f->numTilesY - 1 - tile_y) * f->numTilesX + tile_x : 0;
+    if (f->lastRadiance)
+    {
+        cudaFreeAsync(f->lastRadiance, c->stream);
+        f->lastRadiance = nullptr;
+        f->lastRadianceSamples = 0;
+    }
     lf_status st = run_batch(f, P, sample, 1);
     if (st == LF_OK) f->paths += (uint64_t)f->P.tileW * f->P.tileH;
     return st;
@@ -1077,10 +1011,12 @@ lf_status lf_frame_read_paths(lf_frame* f, float* rgb, int32_t max_samples)
     lf_ctx* c = f->ctx;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     cudaSetDevice(c->device);
-    int n = std::min(max_samples, f->lastBatchSamples);
+    const float4* src = f->lastRadiance ? f->lastRadiance : f->ps.L;
+    int n = std::min(max_samples, f->lastRadiance ? f->lastRadianceSamples : f->lastBatchSamples);
+    if (!src || n <= 0) return fail(c, LF_ERR_STATE, "no rendered paths to read");
     size_t pix = (size_t)f->W * f->H;
     std::vector<float4> tmp(pix * n);
-    cudaError_t e = cudaMemcpyAsync(tmp.data(), f->ps.L, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), src, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "path readback");
     for (size_t i = 0; i < tmp.size(); ++i)
@@ -1125,10 +1061,40 @@ lf_status lf_frame_release(lf_frame* f)
     if (!f) return LF_ERR_INVALID;
     cudaSetDevice(f->ctx->device);
     cudaStreamSynchronize(f->ctx->stream);
+    if (f->lastRadiance)
+    {
+        cudaFreeAsync(f->lastRadiance, f->ctx->stream);
+        cudaStreamSynchronize(f->ctx->stream);
+    }
+    if (f->engineJob >= 0 && f->ctx->engine) engine_job_free(f->ctx->engine, f->engineJob);
     if (f->graph) cudaGraphExecDestroy(f->graph);
     for (void* q : f->allocs) cudaFree(q);
     for (void* q : f->fixedAllocs) cudaFree(q);
     delete f;
+    return LF_OK;
+}
+}
+
+// ------------------------------------------------------------------ engine configuration
+extern "C" {
+lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend, int32_t block_shade,
+                                  int32_t block_shadow, int32_t shade_threads_per_sm)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    EngineHost* e = nullptr;
+    lf_status st = engine_get(c, &e);
+    if (st != LF_OK) return st;
+    return engine_configure(e, slots, block_extend, block_shade, block_shadow, shade_threads_per_sm);
+}
+
+lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes)
+{
+    if (!c || !slots || !device_bytes) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    *slots = c->engine ? c->engine->b.cap : 0;
+    *device_bytes = c->engine ? (int64_t)c->engine->poolBytes : 0;
     return LF_OK;
 }
 }

@@ -504,7 +504,8 @@ lf_status lf_gen_soup(lf_hscene* s, int32_t instances, int32_t tris, uint64_t se
     {
         v.clear();
         n.clear();
-        v3 c(r.uniform() * 100.0f, r.uniform() * 100.0f, r.uniform() * 100.0f);
+        const float cx = r.uniform() * 100.0f, cy = r.uniform() * 100.0f, cz = r.uniform() * 100.0f;
+        const v3 c(cx, cy, cz);   // draws sequenced: argument order is unspecified in C++
         for (int t = 0; t < tris; ++t)
         {
             v3 p[3];
@@ -543,7 +544,8 @@ lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint
     for (int i = 0; i < instances; ++i)
     {
         uint32_t nseed = (uint32_t)(r.next() >> 32);
-        v3 off(r.uniform() * 64.0f, r.uniform() * 64.0f, r.uniform() * 64.0f);
+        const float ox = r.uniform() * 64.0f, oy = r.uniform() * 64.0f, oz = r.uniform() * 64.0f;
+        const v3 off(ox, oy, oz);
         for (size_t k = 0; k < pts.size(); ++k)
         {
             float h = fbm4(pts[k] * 2.0f + off, nseed);
@@ -556,7 +558,8 @@ lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint
         for (size_t k = 0; k < tri.size(); k += 3) push_tri(v, n, disp[tri[k]], disp[tri[k + 1]], disp[tri[k + 2]]);
         int mid = sc.AddMeshData("icosphere", v.data(), n.data(), (int)v.size());
         Material m;
-        m.albedo = Vec3(r.uniform(), r.uniform(), r.uniform());
+        const float ar = r.uniform(), ag = r.uniform(), ab = r.uniform();
+        m.albedo = Vec3(ar, ag, ab);
         m.metallic = r.uniform();
         m.roughness = 0.05f + 0.95f * r.uniform();
         m.transmission = r.uniform() < 0.2f ? 1.0f : 0.0f;
@@ -689,7 +692,8 @@ lf_status lf_gen_rays(const float lo[3], const float hi[3], int64_t nrays, uint6
         float len;
         do
         {
-            d = lfc::v3(r.normal(), r.normal(), r.normal());
+            const float dx = r.normal(), dy = r.normal(), dz = r.normal();
+            d = lfc::v3(dx, dy, dz);
             len = lfc::dot(d, d);
         } while (len < 1e-12f);
         d = lfc::normalize(d);

@@ -130,7 +130,11 @@ float RectIntersect(v3 pos, v3 u, v3 v, v3 n, float planeW, v3 ro, v3 rd)
     return INF_T;
 }
 
-// returns the GLSL value and the entry distance max(t0, 0) used by the optional cull
+// returns the GLSL value and the entry distance max(t0, 0) used by the optional cull; rays
+// with a zero, denormal or non-finite inverse direction component are never culled (their slab
+// values can be NaN or infinite, and the entry is then no lower bound of the hit distance)
+inline bool finite_nonzero(float x) { return std::fabs(x) < 3.0e38f && x != 0.f; }
+
 float AABBIntersect(v3 mn, v3 mx, v3 ro, v3 rd, float* entry)
 {
     v3 invdir = 1.0f / rd;
@@ -140,7 +144,8 @@ float AABBIntersect(v3 mn, v3 mx, v3 ro, v3 rd, float* entry)
     v3 tmin = lfc::vmin(f, n);
     float t1 = lfc::fmin_g(tmax.x, lfc::fmin_g(tmax.y, tmax.z));
     float t0 = lfc::fmax_g(tmin.x, lfc::fmax_g(tmin.y, tmin.z));
-    *entry = t0 > 0.f ? t0 : 0.f;
+    const bool regular = finite_nonzero(invdir.x) && finite_nonzero(invdir.y) && finite_nonzero(invdir.z);
+    *entry = regular && t0 > 0.f ? t0 : 0.f;
     return (t1 >= t0) ? (t0 > 0.f ? t0 : t1) : -1.0f;
 }
 

@@ -129,3 +129,18 @@ CASES = {
     "icospheres_constbg_tiled": 1,
     "icospheres_lens": 1,
 }
+
+
+def stored_params(meta_case):
+    """Render parameters exactly as the golden vectors were made (the camera basis comes from
+    the host's double-precision libm, which may round differently on another host)."""
+    p = lf.RenderParams()
+    for f, _ in p._fields_:
+        v = meta_case["params"][f]
+        if isinstance(v, list):
+            arr = getattr(p, f)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, f, v)
+    return p

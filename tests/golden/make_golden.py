@@ -59,7 +59,9 @@ def main():
         paths = np.zeros((spp, H, W, 3), np.float32)
         sh.refsh_render(C.addressof(view), C.addressof(p), 0, spp, acc.ctypes.data, paths.ctypes.data, 0)
         out[name] = paths
-        meta[name] = {"spp": spp, "width": W, "height": H,
+        params = {f: (list(getattr(p, f)) if hasattr(getattr(p, f), "__len__") else getattr(p, f))
+                  for f, _ in p._fields_}
+        meta[name] = {"spp": spp, "width": W, "height": H, "params": params,
                       "digests": {k: cases.digest(ref_arrays[k]) for k in cases.KEYS},
                       "top_level_index": int(ref_arrays["top_level_index"]),
                       "mean_radiance": float(paths.mean())}

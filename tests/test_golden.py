@@ -27,7 +27,8 @@ def test_scene_arrays_match_reference_digests(name):
 
 @pytest.mark.parametrize("name", sorted(cases.CASES))
 def test_oracle_paths_equal_reference_shader(name):
-    a, p, extras = cases.build(name)
+    a, _, extras = cases.build(name)
+    p = cases.stored_params(META[name])
     view, keep = cases.make_view(a, extras)
     spp = cases.CASES[name]
     acc, paths, _ = oracle.render(view, p, 0, spp, want_paths=True)

@@ -5,6 +5,7 @@ identical; per-path radiance bit-exact (the arithmetic contract makes host and d
 the same IEEE operations), with the 1e-4 relative tolerance of the build plan as the
 reported fallback bar; accumulation buffers identical.
 """
+import json
 import numpy as np
 import pytest
 
@@ -83,6 +84,38 @@ def test_traversal_counters_match_oracle_with_culling(ctx):
     _, ostats = oracle.trace_closest(view, rays, cull_rel=1e-4, cull_abs=cull_abs)
     # inner-node visits and triangle tests: same visit order, same culling
     assert dstats[0] == int(ostats[0]) and dstats[1] == int(ostats[1])
+    ds.close()
+
+
+def axis_rays_on_planes():
+    """Rays with zero direction components whose origins lie on box planes of the Cornell
+    scene: the slab test meets 0 * inf there, so these take the exact (NaN-propagating) box
+    test; the others check the fast one next to it."""
+    coords = np.array([0.0, 0.05, 0.265, 0.5, 0.6, 0.999, 1.0], np.float32)
+    dirs = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (1, 1, 0), (0, -1, 1),
+            (1, 0, -1), (0.3, 0.4, 0.5)]
+    rays = []
+    for x in coords:
+        for y in coords:
+            for z in coords:
+                for d in dirs:
+                    dv = np.array(d, np.float32)
+                    dv = dv / np.float32(np.sqrt(np.float32((dv * dv).sum())))
+                    rays.append([x, y, z, 0, dv[0], dv[1], dv[2], 1e6])
+    return np.array(rays, np.float32)
+
+
+def test_zero_direction_components_match_oracle(ctx):
+    s = scenes.build("cornell")
+    ds = ctx.upload(s)
+    rays = axis_rays_on_planes()
+    for flags in (0, lf.TRACE_SIMPLE):
+        dev = ctx.trace_closest(ds, rays, flags=flags)
+        ref, _ = oracle.trace_closest(s.view(), rays)
+        assert compare_hits(dev, ref) == 0
+        occ = ctx.trace_any(ds, rays, flags=flags)
+        ref_occ, _ = oracle.trace_any(s.view(), rays)
+        assert np.array_equal(occ, ref_occ)
     ds.close()
 
 
@@ -209,7 +242,11 @@ def test_gpu_paths_equal_reference_shader(ctx, name):
     from tests.golden import cases
 
     gold = np.load(ROOT / "tests" / "golden" / "shader_paths.npz")[name]
-    a, p, extras = cases.build(name)
+    meta = json.loads((ROOT / "tests" / "golden" / "scenes.json").read_text())[name]
+    a, _, extras = cases.build(name)
+    for k in cases.KEYS:   # the scene generator is portable: same arrays on this host
+        assert cases.digest(a[k]) == meta["digests"][k], k
+    p = cases.stored_params(meta)
     view, keep = cases.make_view(a, extras)
     ds = lf.DeviceScene(ctx, view)
     f = lf.Frame(ctx, ds, p)
