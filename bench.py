@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--frame-flags", type=int, default=0, help="lf_frame flags of the render workloads (8 = per-batch)")
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (0/512/768)")
-    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full"],
+    ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
+    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
 
@@ -268,6 +269,87 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0):
     return out
 
 
+SERVE_RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080), (2048, 2048)]
+
+
+def serve_scene_pool():
+    """Scenes the serving jobs draw from: the icosphere and room generators at sizes spread
+    log-uniformly over 10k-5M triangles (the Cornell generator has a fixed 34 triangles and
+    does not scale). Built once on the host; the server uploads them on admission."""
+    import lavaframe_gb300 as lf
+
+    pool = []
+    for inst, level in ((1, 5), (4, 6), (13, 6), (64, 6)):           # 20k, 330k, 1.06M, 5.2M tris
+        pool.append(("icospheres", lf.HostScene().gen_icospheres(inst, level, 3, 1024, 512).build()))
+    for boxes in (1000, 16700):                                      # 12k, 200k tris
+        pool.append(("room", lf.HostScene().gen_room(boxes, 4).build()))
+    return pool
+
+
+def serve_jobs(pool, n, seed=11, max_spp=256):
+    """Job list: generator uniform, size log-uniform in [1e4, 5e6] triangles (nearest scene of
+    that generator), resolution, spp U{1..max_spp}, depth U{4..10}, Poisson arrival gaps of
+    rate 20 jobs/s."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for _ in range(n):
+        gen = ["icospheres", "room"][rng.integers(2)]
+        target = np.exp(rng.uniform(np.log(1e4), np.log(5e6)))
+        cands = [(abs(np.log(max(1, int(sc.view().num_tris))) - np.log(target)), k) for k, (g, sc) in enumerate(pool)
+                 if g == gen]
+        scene = min(cands)[1]
+        w, h = SERVE_RESOLUTIONS[rng.integers(len(SERVE_RESOLUTIONS))]
+        jobs.append({"scene": scene, "width": w, "height": h, "spp": int(rng.integers(1, max_spp + 1)),
+                     "depth": int(rng.integers(4, 11)), "gap_s": float(rng.exponential(1.0 / 20.0))})
+    return jobs
+
+
+def run_serving(ctx, n_jobs, max_spp=256):
+    """Serving loop workload: Poisson arrivals into lf_server, then the same jobs submitted at
+    once (batch-only). Returns latency percentiles and throughputs."""
+    import lavaframe_gb300 as lf
+
+    pool = serve_scene_pool()
+    jobs = serve_jobs(pool, n_jobs, max_spp=max_spp)
+
+    def params(j):
+        p = pool[j["scene"]][1].render_params()
+        p.width, p.height, p.max_depth = j["width"], j["height"], j["depth"]
+        return p
+
+    def one_run(arrivals):
+        srv = lf.Server(ctx)
+        sids = [srv.add_scene(sc) for _, sc in pool]
+        t0 = time.perf_counter()
+        ids = []
+        for j in jobs:
+            if arrivals:
+                time.sleep(j["gap_s"])
+            ids.append(srv.submit(sids[j["scene"]], params(j), j["spp"]))
+        for jid in ids:
+            srv.wait(jid)
+        wall = time.perf_counter() - t0
+        infos = [srv.info(jid) for jid in ids]
+        st = srv.stats()
+        for jid in ids:
+            srv.release(jid)
+        srv.close()
+        lat = np.array([i["finish_ms"] - i["submit_ms"] for i in infos])
+        samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+        span = (max(i["finish_ms"] for i in infos) - min(i["submit_ms"] for i in infos)) / 1e3
+        return {"wall_s": wall, "makespan_s": span, "Msamples_per_s": samples / span / 1e6,
+                "ext_rays_per_s": st["ext_rays"] / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+                "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"]}
+
+    serve = one_run(True)
+    batch = one_run(False)
+    return {"jobs": n_jobs, "samples": int(sum(j["width"] * j["height"] * j["spp"] for j in jobs)),
+            "arrival_rate_per_s": 20, "serving": serve, "batch_only": batch,
+            "serving_over_batch": serve["Msamples_per_s"] / batch["Msamples_per_s"],
+            "scenes": [{"generator": g, "triangles": int(sc.view().num_tris)} for g, sc in pool]}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -284,6 +366,13 @@ def main():
     ctx = lf.Context(local)
     if args.engine_slots or args.shade_cap:
         ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap)
+    if args.workload == "c5":
+        r = run_serving(ctx, args.jobs or 48)
+        if rank == 0:
+            print(json.dumps({"metric": "c5 serving Msamples/s", "value": r["serving"]["Msamples_per_s"],
+                              "unit": "Msamples/s", "detail": r}), flush=True)
+        ctx.close()
+        return
     if args.workload != "microbench":
         r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags)
         if rank == 0:

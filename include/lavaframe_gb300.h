@@ -285,6 +285,64 @@ lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, int32_t first_sample, int32_t count,
                             void* d_accum);
 
+/* ------------------------------------------------------------------ serving loop
+ * No counterpart in the reference (one scene per GL context, one frame at a time). A
+ * scheduler thread admits render jobs of registered scenes under a device-memory budget,
+ * keeps scenes resident (uploading on admission, evicting idle scenes least recently used
+ * first) and runs the sample passes of all admitted jobs in the same engine launches, so
+ * jobs that arrive while others run start as soon as memory allows. A job's image is the
+ * one lf_frame_render gives for the same scene, parameters and samples, bit for bit. */
+typedef struct lf_server lf_server;
+
+typedef struct lf_server_config
+{
+    uint64_t memory_budget;    /* device bytes: resident scenes, engine pool, accumulation and
+                                  pass buffers (0 = 150 GiB) */
+    int32_t paths_per_pass;    /* target paths per pass (0 = the engine pool size) */
+    int32_t passes_per_job;    /* passes of one job in flight at once (0 = 2) */
+} lf_server_config;
+
+#define LF_JOB_QUEUED 0
+#define LF_JOB_RUNNING 1
+#define LF_JOB_DONE 2
+#define LF_JOB_FAILED 3
+
+typedef struct lf_job_info
+{
+    int32_t state;             /* LF_JOB_* */
+    int32_t samples_done;      /* samples accumulated so far */
+    double submit_ms, start_ms, finish_ms;   /* server clock: ms since lf_server_create */
+} lf_job_info;
+
+typedef struct lf_server_stats
+{
+    uint64_t jobs_submitted, jobs_done;
+    uint64_t paths, ext_rays, shadow_rays;
+    uint64_t scene_uploads, scene_evictions;
+    uint64_t device_bytes;     /* what the budget counts now */
+    int32_t scenes_resident, jobs_running, jobs_queued;
+} lf_server_stats;
+
+lf_status lf_server_create(lf_ctx* c, const lf_server_config* cfg, lf_server** out);
+/* Registers a scene by its flat arrays; the arrays must stay valid until the scene is
+ * removed (they are uploaded again after an eviction). */
+lf_status lf_server_add_scene(lf_server* s, const lf_scene_view* v, int64_t* scene_id);
+/* LF_ERR_STATE while queued or running jobs use the scene. */
+lf_status lf_server_remove_scene(lf_server* s, int64_t scene_id);
+/* Queues `spp` samples of `p` (samples 0 .. spp-1). LF_ERR_BUDGET if the job could never fit
+ * the budget. */
+lf_status lf_server_submit(lf_server* s, int64_t scene_id, const lf_render_params* p, int32_t spp, int64_t* job_id);
+lf_status lf_server_job_info(lf_server* s, int64_t job_id, lf_job_info* out);
+/* Waits until the job is done or failed; LF_ERR_TIMEOUT after timeout_ms (< 0: no limit). */
+lf_status lf_server_wait(lf_server* s, int64_t job_id, int32_t timeout_ms);
+/* Accumulated radiance sum of a done job, RGB32F, row 0 = bottom. */
+lf_status lf_server_read(lf_server* s, int64_t job_id, float* rgb);
+/* Frees a finished job's buffers (queued jobs are cancelled; running ones: LF_ERR_STATE). */
+lf_status lf_server_release_job(lf_server* s, int64_t job_id);
+lf_status lf_server_get_stats(lf_server* s, lf_server_stats* out);
+/* Stops the scheduler after the running jobs finish; queued jobs are dropped. */
+lf_status lf_server_destroy(lf_server* s);
+
 #ifdef __cplusplus
 }
 #endif

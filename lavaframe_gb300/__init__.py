@@ -94,6 +94,16 @@ _SIG = {
     "lf_frame_set_batch": (C.c_int, [_P, C.c_int32]),
     "lf_frame_release": (C.c_int, [_P]),
     "lf_render_noalloc": (C.c_int, [_P, _P, C.c_int32, C.c_int32, _P]),
+    "lf_server_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "lf_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
+    "lf_server_remove_scene": (C.c_int, [_P, C.c_int64]),
+    "lf_server_submit": (C.c_int, [_P, C.c_int64, _P, C.c_int32, C.POINTER(C.c_int64)]),
+    "lf_server_job_info": (C.c_int, [_P, C.c_int64, _P]),
+    "lf_server_wait": (C.c_int, [_P, C.c_int64, C.c_int32]),
+    "lf_server_read": (C.c_int, [_P, C.c_int64, _F]),
+    "lf_server_release_job": (C.c_int, [_P, C.c_int64]),
+    "lf_server_get_stats": (C.c_int, [_P, _P]),
+    "lf_server_destroy": (C.c_int, [_P]),
 }
 
 
@@ -389,6 +399,88 @@ class DeviceScene:
     def close(self):
         if self.h:
             lib().lf_scene_release(self.h)
+            self.h = _P()
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget", C.c_uint64), ("paths_per_pass", C.c_int32), ("passes_per_job", C.c_int32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("samples_done", C.c_int32), ("submit_ms", C.c_double),
+                ("start_ms", C.c_double), ("finish_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_done", C.c_uint64), ("paths", C.c_uint64),
+                ("ext_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("scene_uploads", C.c_uint64),
+                ("scene_evictions", C.c_uint64), ("device_bytes", C.c_uint64), ("scenes_resident", C.c_int32),
+                ("jobs_running", C.c_int32), ("jobs_queued", C.c_int32)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
+class Server:
+    """Serving loop (lf_server): jobs of registered scenes, continuous batching on the GPU."""
+
+    def __init__(self, ctx: Context, memory_budget=0, paths_per_pass=0, passes_per_job=0):
+        self.ctx = ctx
+        self.h = _P()
+        self._scenes = {}   # id -> HostScene kept alive (the server re-uploads from its arrays)
+        self._dims = {}
+        cfg = ServerConfig(memory_budget, paths_per_pass, passes_per_job)
+        ctx._c(lib().lf_server_create(ctx.h, C.byref(cfg), C.byref(self.h)))
+
+    def add_scene(self, host_scene: "HostScene") -> int:
+        v = host_scene.view()
+        sid = C.c_int64()
+        self.ctx._c(lib().lf_server_add_scene(self.h, C.byref(v), C.byref(sid)))
+        self._scenes[sid.value] = host_scene
+        return sid.value
+
+    def remove_scene(self, sid):
+        self.ctx._c(lib().lf_server_remove_scene(self.h, sid))
+        self._scenes.pop(sid, None)
+
+    def submit(self, sid, params: RenderParams, spp) -> int:
+        jid = C.c_int64()
+        self.ctx._c(lib().lf_server_submit(self.h, sid, C.byref(params), spp, C.byref(jid)))
+        self._dims[jid.value] = (params.height, params.width)
+        return jid.value
+
+    def info(self, jid):
+        out = JobInfo()
+        self.ctx._c(lib().lf_server_job_info(self.h, jid, C.byref(out)))
+        return {"state": out.state, "samples_done": out.samples_done, "submit_ms": out.submit_ms,
+                "start_ms": out.start_ms, "finish_ms": out.finish_ms}
+
+    def wait(self, jid, timeout_ms=-1):
+        """True when done, False on timeout."""
+        st = lib().lf_server_wait(self.h, jid, timeout_ms)
+        if st == 5:
+            return False
+        self.ctx._c(st)
+        return True
+
+    def read(self, jid):
+        h, w = self._dims[jid]
+        out = np.empty((h, w, 3), np.float32)
+        self.ctx._c(lib().lf_server_read(self.h, jid, _fp(out)))
+        return out
+
+    def release(self, jid):
+        self.ctx._c(lib().lf_server_release_job(self.h, jid))
+        self._dims.pop(jid, None)
+
+    def stats(self):
+        out = ServerStats()
+        self.ctx._c(lib().lf_server_get_stats(self.h, C.byref(out)))
+        return {k: getattr(out, k) for k, _ in out._fields_}
+
+    def close(self):
+        if self.h:
+            lib().lf_server_destroy(self.h)
             self.h = _P()
 
 

@@ -137,6 +137,10 @@ inline lf_status check_device(lf_ctx* c)
     return LF_OK;
 }
 
+// Kernel parameters of one render (lf_render_params + scene facts); tile fields cover the
+// whole frame unless the parameters set a tile size.
+void fill_params(Params& P, const lf_render_params* p, const lf_scene* sc);
+
 struct RefNode
 {
     float bmin[3], bmax[3], lr[3];

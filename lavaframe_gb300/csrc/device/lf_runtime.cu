@@ -688,7 +688,8 @@ lf_status lf_trace_stats(const lf_ctx* c, uint64_t out3[3])
 }
 
 // ------------------------------------------------------------------ frames
-namespace
+extern "C++" {
+namespace lfrt
 {
 void fill_params(Params& P, const lf_render_params* p, const lf_scene* sc)
 {
@@ -725,6 +726,11 @@ void fill_params(Params& P, const lf_render_params* p, const lf_scene* sc)
     P.tileOrdinal = 0;
     P.hdrMultiplier = p->hdr_multiplier;
 }
+}
+}   // extern "C++"
+
+namespace
+{
 
 void free_frame_buffers(lf_frame* f)
 {
