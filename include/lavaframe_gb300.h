@@ -343,6 +343,40 @@ lf_status lf_server_get_stats(lf_server* s, lf_server_stats* out);
 /* Stops the scheduler after the running jobs finish; queued jobs are dropped. */
 lf_status lf_server_destroy(lf_server* s);
 
+/* ------------------------------------------------------------------ learned path guiding
+ * No counterpart in the reference (directions come from DisneySample only). A hash-grid +
+ * MLP model (8 levels x 4 FP16 features, 64-64-64-64-48 ReLU network with FP16 weights and
+ * FP32 accumulation on the tensor cores) maps (position, outgoing direction, normal) to an
+ * 8-lobe von Mises-Fisher mixture over incident directions. Trained online with Adam on
+ * directions the tracer sampled, weighted by the luminance they carried over their pdf.
+ * Training sample / query record: 16 floats = position xyz, outgoing direction xyz, normal
+ * xyz, sampled direction xyz, weight, 3 unused. Parameter arrays: 15360 weights (W1 64x64,
+ * W2, W3, W4 48x64, each [out][in]) and 8 x 16384 x 4 grid values. */
+typedef struct lf_guide lf_guide;
+
+#define LF_GUIDE_WEIGHTS 15360
+#define LF_GUIDE_GRID_PARAMS (8 * 16384 * 4)
+#define LF_GUIDE_SAMPLE_FLOATS 16
+#define LF_GUIDE_MIX_FLOATS 40 /* per lobe: mu xyz, kappa, cumulative lobe weight */
+
+/* Positions are normalised to the box [scene_lo, scene_hi]; parameters start from `seed`. */
+lf_status lf_guide_create(lf_ctx* c, const float scene_lo[3], const float scene_hi[3], uint64_t seed,
+                          lf_guide** out);
+lf_status lf_guide_release(lf_guide* g);
+/* FP32 master copies of the parameters (host buffers of LF_GUIDE_WEIGHTS and
+ * LF_GUIDE_GRID_PARAMS floats); setting them also refreshes the FP16 working copies. */
+lf_status lf_guide_get_params(lf_guide* g, float* weights, float* grid);
+lf_status lf_guide_set_params(lf_guide* g, const float* weights, const float* grid);
+/* Loss (mean over the n samples) and its gradients, without changing the parameters. */
+lf_status lf_guide_gradients(lf_guide* g, const float* samples, int32_t n, float* dweights, float* dgrid,
+                             float* loss);
+/* One Adam step (beta 0.9 / 0.99) on n samples in host memory (loss optional) or device memory. */
+lf_status lf_guide_train(lf_guide* g, const float* samples, int32_t n, float lr, float* loss);
+lf_status lf_guide_train_device(lf_guide* g, const float* d_samples, int32_t n, float lr);
+/* Mixture per query (n x LF_GUIDE_MIX_FLOATS, may be NULL) and its pdf at the record's
+ * direction (n floats, may be NULL). */
+lf_status lf_guide_eval(lf_guide* g, const float* queries, int32_t n, float* mix, float* pdf);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,14 @@ _SIG = {
     "lf_server_release_job": (C.c_int, [_P, C.c_int64]),
     "lf_server_get_stats": (C.c_int, [_P, _P]),
     "lf_server_destroy": (C.c_int, [_P]),
+    "lf_guide_create": (C.c_int, [_P, _F, _F, C.c_uint64, C.POINTER(_P)]),
+    "lf_guide_release": (C.c_int, [_P]),
+    "lf_guide_get_params": (C.c_int, [_P, _F, _F]),
+    "lf_guide_set_params": (C.c_int, [_P, _F, _F]),
+    "lf_guide_gradients": (C.c_int, [_P, _F, C.c_int32, _F, _F, _F]),
+    "lf_guide_train": (C.c_int, [_P, _F, C.c_int32, C.c_float, _F]),
+    "lf_guide_train_device": (C.c_int, [_P, _P, C.c_int32, C.c_float]),
+    "lf_guide_eval": (C.c_int, [_P, _F, C.c_int32, _F, _F]),
 }
 
 
@@ -481,6 +489,60 @@ class Server:
     def close(self):
         if self.h:
             lib().lf_server_destroy(self.h)
+            self.h = _P()
+
+
+GUIDE_WEIGHTS = 15360
+GUIDE_GRID_PARAMS = 8 * 16384 * 4
+GUIDE_SAMPLE_FLOATS = 16
+GUIDE_MIX_FLOATS = 40
+
+
+class Guide:
+    """Learned path-guiding model (lf_guide): hash grid + MLP -> vMF mixture, trained on the GPU."""
+
+    def __init__(self, ctx: Context, lo, hi, seed=0):
+        self.ctx = ctx
+        self.h = _P()
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        ctx._c(lib().lf_guide_create(ctx.h, _fp(lo), _fp(hi), seed, C.byref(self.h)))
+
+    def params(self):
+        w = np.empty(GUIDE_WEIGHTS, np.float32)
+        g = np.empty(GUIDE_GRID_PARAMS, np.float32)
+        self.ctx._c(lib().lf_guide_get_params(self.h, _fp(w), _fp(g)))
+        return w, g
+
+    def set_params(self, w, g):
+        w = np.ascontiguousarray(w, np.float32)
+        g = np.ascontiguousarray(g, np.float32)
+        self.ctx._c(lib().lf_guide_set_params(self.h, _fp(w), _fp(g)))
+
+    def gradients(self, samples):
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, GUIDE_SAMPLE_FLOATS)
+        dw = np.empty(GUIDE_WEIGHTS, np.float32)
+        dg = np.empty(GUIDE_GRID_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self.ctx._c(lib().lf_guide_gradients(self.h, _fp(samples), len(samples), _fp(dw), _fp(dg), _fp(loss)))
+        return float(loss[0]), dw, dg
+
+    def train(self, samples, lr=1e-2):
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, GUIDE_SAMPLE_FLOATS)
+        loss = np.zeros(1, np.float32)
+        self.ctx._c(lib().lf_guide_train(self.h, _fp(samples), len(samples), lr, _fp(loss)))
+        return float(loss[0])
+
+    def eval(self, queries):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, GUIDE_SAMPLE_FLOATS)
+        mix = np.empty((len(q), GUIDE_MIX_FLOATS), np.float32)
+        pdf = np.empty(len(q), np.float32)
+        self.ctx._c(lib().lf_guide_eval(self.h, _fp(q), len(q), _fp(mix), _fp(pdf)))
+        return mix, pdf
+
+    def close(self):
+        if self.h:
+            lib().lf_guide_release(self.h)
             self.h = _P()
 
 

@@ -1,0 +1,153 @@
+// Learned path guiding: the model shared by the training and inference kernels (lf_guide.cu)
+// and the guided path kernels. No reference counterpart: the reference samples directions from
+// the BSDF only (disney.glsl:128-225).
+//
+// Model: hash-grid encoding of the position (8 levels x 4 FP16 features) plus one-blob
+// encodings of the outgoing direction and the shading normal (32 values) -> MLP
+// 64-64-64-64-48 with ReLU, FP16 weights, FP32 accumulation on the tensor cores -> 8 von
+// Mises-Fisher lobes (outputs 0..39: mu_raw xyz, kappa_raw, logit per lobe).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace lfd
+{
+namespace guide
+{
+constexpr int kLevels = 8;
+constexpr int kFeatures = 4;
+constexpr int kLog2T = 14;
+constexpr int kT = 1 << kLog2T;
+constexpr int kBlobBins = 8;
+constexpr int kLobes = 8;
+constexpr int kIn = 64;
+constexpr int kHidden = 64;
+constexpr int kOut = 48;          // 40 used
+constexpr int kW1 = 0, kW2 = 64 * 64, kW3 = 2 * 64 * 64, kW4 = 3 * 64 * 64;
+constexpr int kWeights = 3 * 64 * 64 + kOut * 64;   // 15360
+constexpr int kGridParams = kLevels * kT * kFeatures;
+constexpr int kSampleFloats = 16;  // p xyz, wo xyz, n xyz, direction xyz, weight, 3 unused
+constexpr int kMixFloats = 40;     // per query: per lobe mu xyz, kappa, cumulative weight
+constexpr float kBlobSigma = 1.0f / 8.0f;
+
+struct Net
+{
+    const __half* W;      // [W1 | W2 | W3 | W4], each [out][in] row-major
+    const __half* grid;   // [level][entry][feature]
+    int res[kLevels];     // grid resolution per level
+    float lo[3];          // scene box -> [0, 1]^3
+    float invExt[3];
+};
+
+__device__ __forceinline__ uint32_t vertex_index(int res, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint32_t n = (uint32_t)res + 1u;
+    if ((unsigned long long)n * n * n <= (unsigned long long)kT) return x + y * n + z * n * n;
+    return ((x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u)) & (uint32_t)(kT - 1);
+}
+
+// Level l: the 8 corner entries and trilinear weights of position p01 in [0, 1]^3.
+__device__ __forceinline__ void grid_corners(int res, const float p01[3], uint32_t idx[8], float w[8])
+{
+    int i0[3];
+    float fr[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        const float q = fminf(fmaxf(p01[a], 0.f), 1.f) * (float)res;
+        int i = (int)floorf(q);
+        i = i > res - 1 ? res - 1 : i;
+        i0[a] = i;
+        fr[a] = q - (float)i;
+    }
+    for (int c = 0; c < 8; ++c)
+    {
+        const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+        idx[c] = vertex_index(res, (uint32_t)(i0[0] + dx), (uint32_t)(i0[1] + dy), (uint32_t)(i0[2] + dz));
+        w[c] = (dx ? fr[0] : 1.f - fr[0]) * (dy ? fr[1] : 1.f - fr[1]) * (dz ? fr[2] : 1.f - fr[2]);
+    }
+}
+
+__device__ __forceinline__ void sph01(float x, float y, float z, float* th, float* ph)
+{
+    *th = acosf(fminf(fmaxf(z, -1.f), 1.f)) * 0.318309886f;
+    *ph = (atan2f(y, x) + 3.14159265f) * 0.159154943f;
+}
+
+__device__ __forceinline__ float blob(float s, int k)
+{
+    const float c = ((float)k + 0.5f) * (1.0f / kBlobBins);
+    const float u = (s - c) * (1.0f / kBlobSigma);
+    return __expf(-0.5f * u * u);
+}
+
+// Feature f (0..63) of a query: 0..31 grid (level-major), 32..63 one-blob bins.
+__device__ __forceinline__ float grid_feature(const Net& net, const float p01[3], int l, int f)
+{
+    uint32_t idx[8];
+    float w[8];
+    grid_corners(net.res[l], p01, idx, w);
+    const __half* tab = net.grid + (size_t)l * kT * kFeatures;
+    float acc = 0.f;
+    for (int c = 0; c < 8; ++c) acc += w[c] * __half2float(tab[idx[c] * kFeatures + f]);
+    return acc;
+}
+
+__device__ __forceinline__ void position01(const Net& net, const float p[3], float p01[3])
+{
+    for (int a = 0; a < 3; ++a) p01[a] = (p[a] - net.lo[a]) * net.invExt[a];
+}
+
+// von Mises-Fisher lobe parameters from raw outputs (same mapping as the oracle).
+__device__ __forceinline__ void lobe_params(const float* o5, float mu[3], float* kappa)
+{
+    const float nrm = sqrtf(o5[0] * o5[0] + o5[1] * o5[1] + o5[2] * o5[2] + 1e-6f);
+    mu[0] = o5[0] / nrm;
+    mu[1] = o5[1] / nrm;
+    mu[2] = o5[2] / nrm;
+    *kappa = __expf(fminf(fmaxf(o5[3], -3.f), 7.f));
+}
+
+__device__ __forceinline__ float vmf_norm(float k) { return k / (6.28318531f * (1.f - __expf(-2.f * k))); }
+
+// Mixture pdf from the compact per-query form (mu xyz, kappa, cumulative weight per lobe).
+__device__ __forceinline__ float mix_pdf(const float* mix, float wx, float wy, float wz)
+{
+    float p = 0.f, prev = 0.f;
+    for (int i = 0; i < kLobes; ++i)
+    {
+        const float* q = mix + 5 * i;
+        const float pi = q[4] - prev;
+        prev = q[4];
+        const float dot = q[0] * wx + q[1] * wy + q[2] * wz;
+        p += pi * vmf_norm(q[3]) * __expf(q[3] * (dot - 1.f));
+    }
+    return p;
+}
+
+// Samples a direction from the compact mixture with uniforms u0 (lobe), u1, u2.
+__device__ __forceinline__ void mix_sample(const float* mix, float u0, float u1, float u2, float* wx, float* wy,
+                                           float* wz)
+{
+    int i = 0;
+    while (i < kLobes - 1 && u0 > mix[5 * i + 4]) ++i;
+    const float* q = mix + 5 * i;
+    const float k = q[3];
+    // w = 1 + log(u1 + (1 - u1) e^{-2k}) / k  (cosine to the lobe axis)
+    const float w = fminf(fmaxf(1.f + __logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k, -1.f), 1.f);
+    const float s = sqrtf(fmaxf(0.f, 1.f - w * w));
+    float sp, cp;
+    __sincosf(6.28318531f * u2, &sp, &cp);
+    // frame around mu
+    const float mx = q[0], my = q[1], mz = q[2];
+    const float sign = mz >= 0.f ? 1.f : -1.f;
+    const float a = -1.f / (sign + mz);
+    const float b = mx * my * a;
+    const float tx = 1.f + sign * mx * mx * a, ty = sign * b, tz = -sign * mx;
+    const float bx = b, by = sign + my * my * a, bz = -my;
+    *wx = s * cp * tx + s * sp * bx + w * mx;
+    *wy = s * cp * ty + s * sp * by + w * my;
+    *wz = s * cp * tz + s * sp * bz + w * mz;
+}
+}
+}
