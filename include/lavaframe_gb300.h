@@ -376,6 +376,16 @@ lf_status lf_guide_train_device(lf_guide* g, const float* d_samples, int32_t n, 
 /* Mixture per query (n x LF_GUIDE_MIX_FLOATS, may be NULL) and its pdf at the record's
  * direction (n floats, may be NULL). */
 lf_status lf_guide_eval(lf_guide* g, const float* queries, int32_t n, float* mix, float* pdf);
+/* Guided rendering of a frame (g = NULL detaches): at every surface hit a direction comes from
+ * the guide's mixture with probability `alpha` and from DisneySample otherwise, weighted by
+ * one-sample MIS so the estimator stays unbiased; next-event MIS uses the same combined pdf.
+ * Guided frames run the per-batch pipeline in batches of lf_frame_set_batch samples; every
+ * `train_every`-th batch (0 = never) records its path vertices and then trains the guide with
+ * Adam (learning rate `lr`) on the directions they sampled. The guide must outlive the frame's
+ * renders. */
+lf_status lf_frame_set_guide(lf_frame* f, lf_guide* g, float alpha, int32_t train_every, float lr);
+/* Adam steps and training samples used by the frame's guide so far. */
+lf_status lf_frame_guide_stats(lf_frame* f, uint64_t* steps, uint64_t* samples);
 
 #ifdef __cplusplus
 }

@@ -112,6 +112,8 @@ _SIG = {
     "lf_guide_train": (C.c_int, [_P, _F, C.c_int32, C.c_float, _F]),
     "lf_guide_train_device": (C.c_int, [_P, _P, C.c_int32, C.c_float]),
     "lf_guide_eval": (C.c_int, [_P, _F, C.c_int32, _F, _F]),
+    "lf_frame_set_guide": (C.c_int, [_P, _P, C.c_float, C.c_int32, C.c_float]),
+    "lf_frame_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 }
 
 
@@ -586,6 +588,15 @@ class Frame:
 
     def set_batch(self, spp):
         self.ctx._c(lib().lf_frame_set_batch(self.h, spp))
+
+    def set_guide(self, guide, alpha=0.5, train_every=4, lr=1e-2):
+        """Guided rendering with `guide` (None detaches); trains on every train_every-th sample."""
+        self.ctx._c(lib().lf_frame_set_guide(self.h, guide.h if guide else None, alpha, train_every, lr))
+
+    def guide_stats(self):
+        steps, samples = C.c_uint64(), C.c_uint64()
+        self.ctx._c(lib().lf_frame_guide_stats(self.h, C.byref(steps), C.byref(samples)))
+        return {"adam_steps": steps.value, "training_samples": samples.value}
 
     def close(self):
         if self.h:

@@ -426,8 +426,10 @@ __global__ void guide_adam_kernel(float* master, __half* work, float* m, float* 
 
 // Mixture of every query (sample records: p, wo, n) in the compact form used for sampling:
 // per lobe mu xyz, kappa and the cumulative lobe weight.
-__global__ void __launch_bounds__(kWarps * 32) guide_infer_kernel(Net net, const float* queries, int n, float* mix)
+__global__ void __launch_bounds__(kWarps * 32) guide_infer_kernel(Net net, const float* queries, int n,
+                                                                  const int* nDev, float* mix)
 {
+    if (nDev) n = *nDev;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __half* W = reinterpret_cast<__half*>(smem_raw);
     WarpStage* stages = reinterpret_cast<WarpStage*>(smem_raw + sizeof(__half) * kWeights);
@@ -508,6 +510,23 @@ __global__ void to_half_kernel(const float* a, __half* b, int n)
 
 size_t train_smem() { return sizeof(SharedTrain); }
 size_t infer_smem() { return sizeof(__half) * kWeights + sizeof(WarpStage) * kWarps; }
+
+int launch_infer(const Net& net, const float* queries, const int* nDev, int cap, float* mix, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(guide_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem());
+        attr = true;
+    }
+    int sms = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (cap + 15) / 16;
+    const int blocks = std::max(1, std::min(sms * 2, (tiles + kWarps - 1) / kWarps));
+    guide_infer_kernel<<<blocks, kWarps * 32, infer_smem(), st>>>(net, queries, cap, nDev, mix);
+    return (int)cudaGetLastError();
+}
 }
 }
 
@@ -582,6 +601,11 @@ lf_status run_gradients(lf_guide* gd, const float* d_samples, int n)
 }
 
 using namespace guidehost;
+
+namespace lfrt
+{
+lfd::guide::Net guide_net(const lf_guide* g) { return g->net; }
+}
 
 extern "C" {
 
@@ -790,7 +814,7 @@ lf_status lf_guide_eval(lf_guide* gd, const float* queries, int32_t n, float* mi
     }
     const int tiles = (n + 15) / 16;
     guide_infer_kernel<<<std::max(1, std::min(4096, (tiles + kWarps - 1) / kWarps)), kWarps * 32, infer_smem(),
-                         c->stream>>>(gd->net, dq, n, dmix);
+                         c->stream>>>(gd->net, dq, n, nullptr, dmix);
     guide_pdf_kernel<<<grid_blocks(n, 256), 256, 0, c->stream>>>(dmix, dq, n, dpdf);
     if (mix) cudaMemcpyAsync(mix, dmix, (size_t)n * kMixFloats * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (pdf) cudaMemcpyAsync(pdf, dpdf, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream);

@@ -13,10 +13,13 @@
 
 using namespace lfd;
 
+#include "lf_guide.cuh"
+
 namespace lfrt
 {
 struct EngineHost;
 void engine_destroy(EngineHost* e);
+lfd::guide::Net guide_net(const lf_guide* g);
 }
 
 struct lf_ctx
@@ -90,6 +93,19 @@ struct lf_frame
     int engineJob = -1;
     float4* lastRadiance = nullptr;
     int lastRadianceSamples = 0;
+    // learned path guiding (per-batch pipeline, one sample per batch)
+    lf_guide* guide = nullptr;
+    float guideAlpha = 0.5f;
+    int guideTrainEvery = 4;
+    float guideLr = 1e-2f;
+    int guideTrainCap = 1 << 20;
+    int guideBatch = 16384;        // samples per Adam step
+    long long guideCap = 0;        // path slots the guide buffers hold
+    GuideBuffers gb{};
+    std::vector<void*> guideAllocs;
+    uint64_t guideSteps = 0;
+    uint64_t guideSamples = 0;
+    uint64_t guideBatches = 0;     // guided batches rendered (training cadence)
 };
 
 namespace lfrt

@@ -308,6 +308,115 @@ __global__ void trace_any_kernel(DevScene S, const float4* rays, long long n, ui
     }
 }
 
+// ------------------------------------------------------------------ guided bounces
+// Query record (position, outgoing direction, shading normal) of every queued path that hit a
+// triangle; other entries get a zero record (their mixture is computed and not used).
+__global__ void guide_query_kernel(ShadeScene S, PathSoA ps, const int* queue, const int* qcount, float* queries)
+{
+    const int n = *qcount;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int p = queue[i];
+        const float4 h = ps.hit[p];
+        float* q = queries + (size_t)i * guide::kSampleFloats;
+        float v[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 1.f};
+        const int prim = __float_as_int(h.z), light = __float_as_int(h.w);
+        if (h.x != kInfinity && light < 0 && prim >= 0)
+        {
+            const float4 o4 = ps.o[p], d4 = ps.d[p];
+            const SurfaceGeom g = surface_geom(S, f3(o4), f3(d4), h.x, __float_as_int(h.y), prim);
+            const float vv[9] = {g.fhp.x, g.fhp.y, g.fhp.z, -d4.x, -d4.y, -d4.z, g.nrm.x, g.nrm.y, g.nrm.z};
+            for (int k = 0; k < 9; ++k) v[k] = vv[k];
+        }
+        for (int k = 0; k < 9; ++k) q[k] = v[k];
+    }
+}
+
+__global__ void __launch_bounds__(128, 4) shade_guided_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin,
+                                                               const int* qinCount, int* qout, int* qoutCount,
+                                                               ShadowRec* sq, int* sqCount, int cap, uint32_t* status,
+                                                               unsigned long long* ctr, GuideCtx gc)
+{
+    const int n = *qinCount;
+    const int stride = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int warpBase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+    for (int base = warpBase; base < n; base += stride)
+    {
+        int i = base + lane;
+        bool pushExt = false, pushShadow = false;
+        int p = -1;
+        ShadowRec rec;
+        if (i < n)
+        {
+            p = qin[i];
+            shade_path_t<true>(S, P, ps, p, ctr, pushExt, pushShadow, rec, gc, i);
+        }
+        warp_push(pushExt, p, qout, qoutCount, cap, status);
+        warp_push(pushShadow, rec, sq, sqCount, cap, status);
+    }
+}
+
+// Training samples of the batch: for every recorded vertex k of a path (all but the path's
+// last vertex), the radiance its sampled direction carried is (L_final - L_start(k+1)) /
+// throughput after k; the sample weight is its luminance over the direction's pdf.
+__global__ void guide_collect_kernel(PathSoA ps, GuideBuffers g, long long n)
+{
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n; base += stride)
+    {
+        const long long p = base + lane;
+        int depth = 0;
+        float4 Lf = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p < n && ps.info[p].x >= 0)
+        {
+            depth = ps.info[p].y;
+            Lf = ps.L[p];
+        }
+        const int maxK = __reduce_max_sync(kFull, (unsigned)(depth > 1 ? depth - 1 : 0));
+        for (int k = 0; k < maxK; ++k)
+        {
+            bool take = false;
+            float smp[13];
+            if (k < depth - 1)
+            {
+                const float* r = g.rec + ((size_t)p * g.maxDepth + k) * kGuideRecFloats;
+                if (r[19] == 2.f && r[12] > 0.f)
+                {
+                    const float lx = r[13] > 0.f ? (Lf.x - r[16]) / r[13] : 0.f;
+                    const float ly = r[14] > 0.f ? (Lf.y - r[17]) / r[14] : 0.f;
+                    const float lz = r[15] > 0.f ? (Lf.z - r[18]) / r[15] : 0.f;
+                    const float lum = 0.2126f * lx + 0.7152f * ly + 0.0722f * lz;
+                    const float w = fminf(lum / r[12], g.weightClamp);
+                    if (w > 0.f && w == w)
+                    {
+                        for (int c = 0; c < 12; ++c) smp[c] = r[c];
+                        smp[12] = w;
+                        take = true;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(kFull, take);
+            if (!m) continue;
+            const int leader = __ffs(m) - 1;
+            int pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(g.trainCount, __popc(m));
+            pos0 = __shfl_sync(kFull, pos0, leader);
+            if (take)
+            {
+                const int pos = pos0 + __popc(m & ((1u << lane) - 1u));
+                if (pos < g.trainCap)
+                {
+                    float* dst = g.train + (size_t)pos * guide::kSampleFloats;
+                    for (int c = 0; c < 13; ++c) dst[c] = smp[c];
+                    dst[13] = dst[14] = dst[15] = 0.f;
+                }
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ launchers
 namespace
 {
@@ -375,6 +484,34 @@ int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const
         int gw = grid_for((const void*)shadow_kernel, BW, cap);
         shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.status, b.ctr);
     }
+    return (int)cudaGetLastError();
+}
+
+int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps, const BounceBuffers& b,
+                         const GuideBuffers& g, int bounce, long long cap, cudaStream_t st)
+{
+    int* qin = b.queue[bounce & 1];
+    int* qout = b.queue[(bounce + 1) & 1];
+    int* cin = b.count + (bounce & 1);
+    int* cout = b.count + ((bounce + 1) & 1);
+    cudaMemsetAsync(cout, 0, sizeof(int), st);
+    cudaMemsetAsync(b.shadowCount, 0, sizeof(int), st);
+    const int B = 128;
+    extend_kernel<<<grid_for((const void*)extend_kernel, B, cap), B, 0, st>>>(S, P, ps, qin, cin, b.status, b.ctr);
+    guide_query_kernel<<<grid_for((const void*)guide_query_kernel, B, cap), B, 0, st>>>(S, ps, qin, cin, g.queries);
+    int e = guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
+    if (e) return e;
+    GuideCtx gc{g.mix, g.rec, g.alpha, g.maxDepth};
+    shade_guided_kernel<<<grid_for((const void*)shade_guided_kernel, B, cap), B, 0, st>>>(
+        S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr, gc);
+    shadow_kernel<<<grid_for((const void*)shadow_kernel, B, cap), B, 0, st>>>(S, P, ps, b.shadow, b.shadowCount,
+                                                                             b.status, b.ctr);
+    return (int)cudaGetLastError();
+}
+
+int launch_guide_collect(const PathSoA& ps, const GuideBuffers& g, long long n, cudaStream_t st)
+{
+    guide_collect_kernel<<<grid_for((const void*)guide_collect_kernel, 256, n), 256, 0, st>>>(ps, g, n);
     return (int)cudaGetLastError();
 }
 

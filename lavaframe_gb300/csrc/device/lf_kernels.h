@@ -1,6 +1,7 @@
 // Launch interface of the wavefront kernels and ray queries (implemented in lf_kernels.cu).
 #pragma once
 
+#include "lf_guide.cuh"
 #include "lf_shade.cuh"
 
 namespace lfd
@@ -41,6 +42,30 @@ struct BounceBuffers
     unsigned long long* ctr;   // [0] paths, [1] extension rays, [2] shadow rays, [3] light clamps
     unsigned long long* fetch; // [2] work counters of the persistent extend / shadow kernels
 };
+
+// Floats per recorded path vertex of guided rendering (see GuideCtx in lf_pathops.cuh).
+constexpr int kGuideRecFloats = 20;
+
+// Guided bounces (learned path guiding): per-queue-position queries and mixtures, per-slot
+// training records, and the training sample buffer of the batch.
+struct GuideBuffers
+{
+    guide::Net net;
+    float* queries;      // cap x guide::kSampleFloats
+    float* mix;          // cap x guide::kMixFloats
+    float* rec;          // cap x maxDepth x 20, or null when the batch is not recorded
+    float* train;        // trainCap x guide::kSampleFloats
+    int* trainCount;
+    int trainCap;
+    float alpha;         // mixture selection probability
+    int maxDepth;
+    float weightClamp;   // training weights are clamped to this
+};
+
+int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps, const BounceBuffers& b,
+                         const GuideBuffers& g, int bounce, long long cap, cudaStream_t st);
+// Training samples from the recorded vertices of the batch's n paths.
+int launch_guide_collect(const PathSoA& ps, const GuideBuffers& g, long long n, cudaStream_t st);
 
 int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,
                     int* queue, int* qcount, cudaStream_t st);

@@ -3,6 +3,7 @@
 // surface / miss / emitter shading with next-event candidates, and next-event visibility.
 #pragma once
 
+#include "lf_guide.cuh"
 #include "lf_kernels.h"
 
 namespace lfd
@@ -139,11 +140,61 @@ __device__ __forceinline__ void gen_path(const Params& P, int tileX, int tileY, 
     ps.luv[slot] = make_float2(0.f, 0.f);
 }
 
+// Position and interpolated shading normal (before normal mapping) of a triangle hit, as in
+// GetNormalsAndTexCoord (pathtrace.glsl:16-37).
+struct SurfaceGeom
+{
+    v3 fhp;          // world hit point
+    v3 nrm;          // world shading normal
+    lfc::v2 texCoord;
+    int material;
+};
+
+__device__ __forceinline__ SurfaceGeom surface_geom(const ShadeScene& S, v3 o, v3 d, float t, int inst, int prim)
+{
+    float m[12];
+    int root, matId;
+    load_instance(S.trav.instances + (size_t)inst * 4, m, &root, &matId);
+    const ShadeInstance& SI = S.inst[inst];
+    v3 ro = xform(m, o, 1.0f), rd = xform(m, d, 0.0f);
+    float u, v;
+    tri_hit(S.trav.tris + (size_t)prim * 3, ro, rd, &u, &v);
+    float bw = 1.0f - u - v;
+    SurfaceGeom g;
+    g.fhp = xform(SI.fwd, ro + rd * t, 1.0f);
+    int4 vi = S.vertIndices[prim];
+    float4 n1 = S.normals[vi.x], n2 = S.normals[vi.y], n3 = S.normals[vi.z];
+    float w0 = S.vertices[vi.x].w, w1 = S.vertices[vi.y].w, w2 = S.vertices[vi.z].w;
+    g.texCoord = lfc::v2(w0, n1.w) * bw + lfc::v2(w1, n2.w) * u + lfc::v2(w2, n3.w) * v;
+    v3 nrm = lfc::normalize(pathops::f3(n1) * bw + pathops::f3(n2) * u + pathops::f3(n3) * v);
+    g.nrm = lfc::normalize(lfc::mul3(SI.nrm, nrm));
+    g.material = SI.material;
+    return g;
+}
+
+// Guided sampling state of one bounce (learned path guiding; no reference counterpart).
+// mix: the mixture of each queue position; rec: per path slot, maxDepth training records of
+// kGuideRecFloats (hit point, outgoing direction, normal, sampled direction, pdf, throughput
+// after the vertex, radiance at the next vertex's start, state).
+struct GuideCtx
+{
+    const float* mix;
+    float* rec;
+    float alpha;     // probability of sampling the mixture instead of the BSDF
+    int maxDepth;
+};
+
 // One bounce of PathTrace for the path in slot p after its closest hit is known
 // (pathtrace.glsl:208-294 minus the visibility tests): returns whether the path continues
 // (pushExt) and whether it has next-event rays (pushShadow, described by rec).
-__device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
-                                           unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec)
+// kGuided: directions come from the learned mixture with probability alpha and from the BSDF
+// otherwise (one-sample MIS: the pdf is alpha * p_mix + (1 - alpha) * p_bsdf, the BSDF value
+// DisneyEval's), the same combined pdf weighs next-event estimation, and the vertex is
+// recorded for training; qpos is the path's queue position (index of its mixture).
+template <bool kGuided>
+__device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
+                                             unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec,
+                                             const GuideCtx& gc, int qpos)
 {
     using namespace pathops;
     float4 o4 = ps.o[p], d4 = ps.d[p], T4 = ps.T[p], L4 = ps.L[p], A4 = ps.A[p], h = ps.hit[p];
@@ -155,6 +206,16 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
     const int depth = info.y;
     const float t = h.x;
     const int inst = __float_as_int(h.y), prim = __float_as_int(h.z), light = __float_as_int(h.w);
+    if (kGuided && gc.rec && depth > 0)
+    {
+        // radiance at the start of this vertex: everything the previous vertex's direction
+        // has not carried yet
+        float* r = gc.rec + ((size_t)p * gc.maxDepth + depth - 1) * kGuideRecFloats;
+        r[16] = L.x;
+        r[17] = L.y;
+        r[18] = L.z;
+        r[19] = 2.f;
+    }
 
     if (t == kInfinity)
     {
@@ -199,30 +260,21 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
     else
     {
         // ---- GetNormalsAndTexCoord (pathtrace.glsl:16-37)
-        float m[12];
-        int root, matId;
-        load_instance(S.trav.instances + (size_t)inst * 4, m, &root, &matId);
-        const ShadeInstance& SI = S.inst[inst];
-        v3 ro = xform(m, o, 1.0f), rd = xform(m, d, 0.0f);
-        float u, v;
-        tri_hit(S.trav.tris + (size_t)prim * 3, ro, rd, &u, &v);
-        float bw = 1.0f - u - v;
-        v3 fhp = xform(SI.fwd, ro + rd * t, 1.0f);
-        int4 vi = S.vertIndices[prim];
-        float4 n1 = S.normals[vi.x], n2 = S.normals[vi.y], n3 = S.normals[vi.z];
-        float w0 = S.vertices[vi.x].w, w1 = S.vertices[vi.y].w, w2 = S.vertices[vi.z].w;
+        const SurfaceGeom geo = surface_geom(S, o, d, t, inst, prim);
+        const v3 fhp = geo.fhp;
+        const v3 nrm = geo.nrm;
         Surf s;
-        s.texCoord = lfc::v2(w0, n1.w) * bw + lfc::v2(w1, n2.w) * u + lfc::v2(w2, n3.w) * v;
-        v3 nrm = lfc::normalize(f3(n1) * bw + f3(n2) * u + f3(n3) * v);
-        nrm = lfc::normalize(lfc::mul3(SI.nrm, nrm));
+        s.texCoord = geo.texCoord;
         s.normal = nrm;
         s.ffnormal = lfc::dot(nrm, d) <= 0.0f ? nrm : nrm * -1.0f;
         Onb(s.normal, s.tangent, s.bitangent);
         // ---- GetMaterialsAndTextures (pathtrace.glsl:40-123)
-        s.mat = load_material(S, SI.material);
+        s.mat = load_material(S, geo.material);
         apply_textures(S, s, d);
         s.eta = lfc::dot(d, s.normal) < 0.0f ? (1.0f / s.mat.ior) : s.mat.ior;
-        info.z = SI.material;
+        info.z = geo.material;
+        const float* mix = kGuided ? gc.mix + (size_t)qpos * guide::kMixFloats : nullptr;
+        const float alpha = kGuided ? gc.alpha : 0.f;
         ps.luv[p] = make_float2(s.texCoord.x, s.texCoord.y);
 
         if (lfc::dot(s.normal, s.ffnormal) > 0.0f) A = v3(0.0f);
@@ -246,7 +298,9 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
             v3 f = DisneyEval(bc, V, s.ffnormal, envDir, pdf);
             if (pdf > 0.0f)
             {
-                float mis = powerHeuristic(lightPdf, pdf);
+                const float dirPdf =
+                    kGuided ? alpha * guide::mix_pdf(mix, envDir.x, envDir.y, envDir.z) + (1.0f - alpha) * pdf : pdf;
+                float mis = powerHeuristic(lightPdf, dirPdf);
                 if (mis > 0.0f)
                 {
                     envC = mis * f * fabsf(lfc::dot(envDir, s.ffnormal)) * color / lightPdf;
@@ -297,7 +351,9 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
                 float pdf;
                 v3 f = DisneyEval(bc, V, s.ffnormal, ldir, pdf);
                 float weight = 1.0f;
-                if (Lt.area > 0.0f) weight = powerHeuristic(lpdf, pdf);
+                const float dirPdf =
+                    kGuided ? alpha * guide::mix_pdf(mix, ldir.x, ldir.y, ldir.z) + (1.0f - alpha) * pdf : pdf;
+                if (Lt.area > 0.0f) weight = powerHeuristic(lpdf, dirPdf);
                 if (pdf > 0.0f)
                 {
                     lightC = weight * f * fabsf(lfc::dot(s.ffnormal, ldir)) * lem / lpdf;
@@ -323,7 +379,22 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
         // ---- DisneySample, absorption, throughput, RR (pathtrace.glsl:268-291)
         v3 Ls;
         float pdf;
-        v3 f = DisneySample(bc, rng, V, s.ffnormal, Ls, pdf);
+        v3 f;
+        if (kGuided)
+        {
+            if (rnd(rng) < alpha)
+            {
+                const float u0 = rnd(rng), u1 = rnd(rng), u2 = rnd(rng);
+                guide::mix_sample(mix, u0, u1, u2, &Ls.x, &Ls.y, &Ls.z);
+            }
+            else
+                DisneySample(bc, rng, V, s.ffnormal, Ls, pdf);
+            float bsdfPdfL;
+            f = DisneyEval(bc, V, s.ffnormal, Ls, bsdfPdfL);
+            pdf = alpha * guide::mix_pdf(mix, Ls.x, Ls.y, Ls.z) + (1.0f - alpha) * bsdfPdfL;
+        }
+        else
+            f = DisneySample(bc, rng, V, s.ffnormal, Ls, pdf);
         if (lfc::dot(s.ffnormal, Ls) < 0.0f) A = (-lfc::vlog(s.mat.extinction)) / s.mat.atDistance;
         bool alive = true;
         if (pdf > 0.0f)
@@ -342,6 +413,14 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
             o = fhp + d * kEps;
             if (depth + 1 < P.maxDepth) pushExt = true;
         }
+        if (kGuided && gc.rec && depth < gc.maxDepth)
+        {
+            float* r = gc.rec + ((size_t)p * gc.maxDepth + depth) * kGuideRecFloats;
+            const float vals[16] = {fhp.x, fhp.y, fhp.z, V.x, V.y, V.z, nrm.x, nrm.y, nrm.z,
+                                    Ls.x,  Ls.y,  Ls.z,  pdf, T.x, T.y, T.z};
+            for (int k = 0; k < 16; ++k) r[k] = vals[k];
+            r[19] = pushExt ? 1.f : 0.f;
+        }
         info.y = depth + 1;
         ps.o[p] = f4(o, pdf);
         ps.d[p] = f4(d, 0.f);
@@ -351,6 +430,12 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
         ps.rng[p] = make_uint4(rng.x, rng.y, rng.z, rng.w);
         ps.info[p] = info;
     }
+}
+
+__device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
+                                           unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec)
+{
+    shade_path_t<false>(S, P, ps, p, ctr, pushExt, pushShadow, rec, GuideCtx{nullptr, nullptr, 0.f, 0}, 0);
 }
 
 // Visibility of a path's next-event rays, then radiance += Li * throughput

@@ -865,8 +865,9 @@ lf_status end_batch_graph(lf_frame* f, cudaError_t launchErr, const char* what)
     return LF_OK;
 }
 
-// One batch of samples on one tile: generate, maxDepth bounces, accumulate.
-lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
+// One batch of samples on one tile: generate, maxDepth bounces, accumulate. With a guide,
+// `record` keeps the batch's path vertices and collects training samples.
+lf_status run_batch(lf_frame* f, Params P, int firstSample, int n, bool record = false)
 {
     lf_ctx* c = f->ctx;
     const ShadeScene& S = f->scene->view;
@@ -896,11 +897,119 @@ lf_status run_batch(lf_frame* f, Params P, int firstSample, int n)
     // icosphere scenes; LF_WAVEFRONT_PERSISTENT=1 selects the persistent extend/shadow kernels.
     static const bool persistent = std::getenv("LF_WAVEFRONT_PERSISTENT") != nullptr;
     if (!persistent) bb.fetch = nullptr;
-    for (int b = 0; b < P.maxDepth && !e; ++b) e = launch_bounce(Sv, P, f->ps, bb, b, cap, c->stream);
+    if (f->guide)
+    {
+        GuideBuffers gb = f->gb;
+        gb.net = guide_net(f->guide);
+        gb.rec = record ? f->gb.rec : nullptr;
+        for (int b = 0; b < P.maxDepth && !e; ++b) e = launch_bounce_guided(Sv, P, f->ps, bb, gb, b, cap, c->stream);
+        if (!e && record)
+        {
+            cudaMemsetAsync(gb.trainCount, 0, sizeof(int), c->stream);
+            e = launch_guide_collect(f->ps, gb, cap, c->stream);
+        }
+    }
+    else
+        for (int b = 0; b < P.maxDepth && !e; ++b) e = launch_bounce(Sv, P, f->ps, bb, b, cap, c->stream);
     if (!e) e = launch_accumulate(P, f->ps, n, f->accum, f->accum64, c->stream);
     f->lastBatchSamples = n;
     if (graph) return end_batch_graph(f, (cudaError_t)e, "batch launch");
     if (e) return cuda_fail(c, (cudaError_t)e, "batch launch");
+    return LF_OK;
+}
+}
+
+namespace
+{
+void free_guide_buffers(lf_frame* f)
+{
+    for (void* q : f->guideAllocs) cudaFree(q);
+    f->guideAllocs.clear();
+    f->guideCap = 0;
+    f->gb = GuideBuffers{};
+}
+
+lf_status alloc_guide_buffers(lf_frame* f, long long cap)
+{
+    free_guide_buffers(f);
+    size_t bytes = 0;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto** q, size_t n) {
+        if (e == cudaSuccess) e = dalloc(f->guideAllocs, bytes, q, n);
+    };
+    const int depth = std::max(1, f->P.maxDepth);
+    A(&f->gb.queries, (size_t)cap * guide::kSampleFloats);
+    A(&f->gb.mix, (size_t)cap * guide::kMixFloats);
+    A(&f->gb.rec, (size_t)cap * depth * kGuideRecFloats);
+    A(&f->gb.train, (size_t)f->guideTrainCap * guide::kSampleFloats);
+    A(&f->gb.trainCount, 1);
+    if (e != cudaSuccess)
+    {
+        free_guide_buffers(f);
+        return cuda_fail(f->ctx, e, "guide buffers");
+    }
+    f->gb.trainCap = f->guideTrainCap;
+    f->gb.alpha = f->guideAlpha;
+    f->gb.maxDepth = depth;
+    f->gb.weightClamp = 1e4f;
+    f->guideCap = cap;
+    return LF_OK;
+}
+
+// Guided batches of up to sppBatch samples (every tile); every train_every-th batch records
+// its path vertices and trains the guide afterwards (Adam steps of guideBatch samples over
+// what it collected).
+lf_status frame_render_guided(lf_frame* f, Params P, int firstSample, int count)
+{
+    lf_ctx* c = f->ctx;
+    const long long tilePix = (long long)P.tileW * P.tileH;
+    const long long cap = (long long)std::max(1, f->sppBatch) * tilePix;
+    if (f->guideCap < cap)
+    {
+        lf_status st = alloc_guide_buffers(f, cap);
+        if (st != LF_OK) return st;
+    }
+    if (f->lastRadiance)
+    {
+        cudaFreeAsync(f->lastRadiance, c->stream);
+        f->lastRadiance = nullptr;
+        f->lastRadianceSamples = 0;
+    }
+    const bool tiledFrames = (f->flags & LF_FRAME_TILED_FRAMES) != 0;
+    for (int s = 0; s < count;)
+    {
+        const int n = std::min(std::max(1, f->sppBatch), count - s);
+        const bool record = f->guideTrainEvery > 0 && f->guideBatches % (uint64_t)f->guideTrainEvery == 0;
+        ++f->guideBatches;
+        for (int ty = f->numTilesY - 1; ty >= 0; --ty)
+            for (int tx = 0; tx < f->numTilesX; ++tx)
+            {
+                P.tileX = tx;
+                P.tileY = ty;
+                P.tileOrdinal = tiledFrames ? (f->numTilesY - 1 - ty) * f->numTilesX + tx : 0;
+                lf_status st = run_batch(f, P, firstSample + s, n, record);
+                if (st != LF_OK) return st;
+                if (!record) continue;
+                int collected = 0;
+                cudaError_t e = cudaMemcpyAsync(&collected, f->gb.trainCount, sizeof(int), cudaMemcpyDeviceToHost,
+                                                c->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+                if (e != cudaSuccess) return cuda_fail(c, e, "guide sample count");
+                const int avail = std::min(collected, f->gb.trainCap);
+                const int steps = std::min(64, (avail + f->guideBatch - 1) / f->guideBatch);
+                for (int k = 0; k < steps; ++k)
+                {
+                    const int off = k * f->guideBatch;
+                    const int nb = std::min(f->guideBatch, avail - off);
+                    st = lf_guide_train_device(f->guide, f->gb.train + (size_t)off * guide::kSampleFloats, nb,
+                                               f->guideLr);
+                    if (st != LF_OK) return st;
+                    f->guideSteps++;
+                    f->guideSamples += (uint64_t)nb;
+                }
+            }
+        s += n;
+    }
     return LF_OK;
 }
 }
@@ -914,6 +1023,13 @@ lf_status lf_frame_render(lf_frame* f, int32_t first_sample, int32_t count)
     Params P = f->P;
     const bool tiledFrames = (f->flags & LF_FRAME_TILED_FRAMES) != 0;
     P.frameStride = tiledFrames ? f->numTilesX * f->numTilesY : 1;
+    if (f->guide)
+    {
+        if (count == 0) return LF_OK;
+        lf_status st = frame_render_guided(f, P, first_sample, count);
+        if (st == LF_OK) f->paths += (uint64_t)count * f->W * f->H;
+        return st;
+    }
     if (!(f->flags & LF_FRAME_PER_BATCH))
     {
         if (count == 0) return LF_OK;
@@ -1062,6 +1178,31 @@ lf_status lf_frame_counters(lf_frame* f, uint64_t out4[4])
     return LF_OK;
 }
 
+lf_status lf_frame_set_guide(lf_frame* f, lf_guide* g, float alpha, int32_t train_every, float lr)
+{
+    if (!f || train_every < 0 || (g && !(alpha > 0.f && alpha < 1.f)) || (g && train_every > 0 && !(lr > 0.f)))
+        return LF_ERR_INVALID;
+    lf_ctx* c = f->ctx;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    f->guide = g;
+    f->guideAlpha = alpha;
+    f->guideTrainEvery = train_every;
+    f->guideLr = lr;
+    f->gb.alpha = alpha;
+    if (!g) free_guide_buffers(f);
+    return LF_OK;
+}
+
+lf_status lf_frame_guide_stats(lf_frame* f, uint64_t* steps, uint64_t* samples)
+{
+    if (!f || !steps || !samples) return LF_ERR_INVALID;
+    *steps = f->guideSteps;
+    *samples = f->guideSamples;
+    return LF_OK;
+}
+
 lf_status lf_frame_release(lf_frame* f)
 {
     if (!f) return LF_ERR_INVALID;
@@ -1073,6 +1214,7 @@ lf_status lf_frame_release(lf_frame* f)
         cudaStreamSynchronize(f->ctx->stream);
     }
     if (f->engineJob >= 0 && f->ctx->engine) engine_job_free(f->ctx->engine, f->engineJob);
+    free_guide_buffers(f);
     if (f->graph) cudaGraphExecDestroy(f->graph);
     for (void* q : f->allocs) cudaFree(q);
     for (void* q : f->fixedAllocs) cudaFree(q);

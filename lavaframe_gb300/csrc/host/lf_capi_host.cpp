@@ -652,9 +652,12 @@ lf_status lf_gen_room(lf_hscene* s, int32_t boxes, uint64_t seed)
         int nb = boxes - b0 < perMesh ? boxes - b0 : perMesh;
         for (int b = 0; b < nb; ++b)
         {
-            float sx = 0.05f + 0.25f * r.uniform(), sy = 0.05f + 0.6f * r.uniform(), sz = 0.05f + 0.25f * r.uniform();
+            // small clutter (2-14 cm wide, up to 30 cm high), so that 200k triangles leave the
+            // room navigable for light entering through the doorway
+            float sx = 0.02f + 0.12f * r.uniform(), sy = 0.02f + 0.28f * r.uniform(), sz = 0.02f + 0.12f * r.uniform();
             float x = 0.3f + (9.4f - sx) * r.uniform(), z = 0.3f + (9.4f - sz) * r.uniform();
-            float y = r.uniform() < 0.7f ? 0.0f : 0.3f + 3.0f * r.uniform();
+            if (x > 8.0f && z > 3.5f && z < 6.5f) x = x - 7.5f;   // keep the way to the doorway clear
+            float y = r.uniform() < 0.9f ? 0.0f : 0.3f + 3.0f * r.uniform();
             push_box(v, n, v3(x, y, z), v3(x + sx, y + sy, z + sz));
         }
         int mid = sc.AddMeshData("furniture", v.data(), n.data(), (int)v.size());
