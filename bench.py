@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (0/512/768)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
-    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c5"],
+    ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
+    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
 
@@ -238,7 +239,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which, spp=None, spp_batch=0, flags=0):
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False):
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -249,6 +250,11 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0):
         spp = spp or 16
     p = s.render_params()
     ds = ctx.upload(s)
+    tuned = None
+    if tune:
+        from lavaframe_gb300 import autotune
+
+        tuned = autotune.tune(ctx, ds, p, spp=4, triangles=int(s.view().num_tris))
     f = lf.Frame(ctx, ds, p, flags)
     if spp_batch:
         f.set_batch(spp_batch)
@@ -264,6 +270,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0):
            "shadow_rays_per_s": ctr[2] / (ms / 1e3), "ms": ms, "spp": spp,
            "resolution": [p.width, p.height], "max_depth": p.max_depth,
            "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1])}
+    if tuned:
+        out["autotuned"] = {"config": tuned["config"], "trials": len(tuned["trials"])}
     f.close()
     ds.close()
     return out
@@ -350,6 +358,75 @@ def run_serving(ctx, n_jobs, max_spp=256):
             "scenes": [{"generator": g, "triangles": int(sc.view().num_tris)} for g, sc in pool]}
 
 
+def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=4, every=2, max_factor=3.0):
+    """Time-to-error of learned path guiding on the occluded-light room (16.7k boxes, ~200k
+    triangles, depth 10): the plain tracer's error after plain_spp samples, against an FP64
+    reference of ref_spp samples, and the wall time the guided tracer (trained online, Adam
+    every `every`-th batch of `batch` samples) needs to reach the same error."""
+    import lavaframe_gb300 as lf
+
+    s = lf.HostScene().gen_room(16700, 4).build()
+    a = s.arrays()
+    top = int(a["top_level_index"])
+    lo, hi = a["nodes"][top][0:3], a["nodes"][top][3:6]
+    p = s.render_params()
+    p.width, p.height = width, height
+    ds = ctx.upload(s)
+
+    def frame():
+        return lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM)
+
+    f = frame()
+    f.set_batch(16)
+    t0 = time.perf_counter()
+    f.render(0, ref_spp)
+    f.sync()
+    t_ref = time.perf_counter() - t0
+    ref = f.accum64() / ref_spp
+    f.close()
+
+    def rmse(img):
+        return float(np.sqrt(((img - ref) ** 2).mean()))
+
+    f = frame()
+    f.render(1 << 20, 8)
+    f.sync()
+    f.reset()
+    t0 = time.perf_counter()
+    f.render(1 << 20, plain_spp)
+    f.sync()
+    t_plain = time.perf_counter() - t0
+    target = rmse(f.accum64() / plain_spp)
+    f.close()
+
+    g = lf.Guide(ctx, lo, hi, seed=1)
+    f = frame()
+    f.set_batch(batch)
+    f.set_guide(g, 0.5, every, 1e-2)
+    spent, done, reached, last = 0.0, 0, False, None
+    while spent < max_factor * t_plain:
+        t0 = time.perf_counter()
+        f.render((1 << 20) + done, batch)
+        f.sync()
+        spent += time.perf_counter() - t0
+        done += batch
+        if done % 16 == 0:
+            last = rmse(f.accum64() / done)
+            if last <= target:
+                reached = True
+                break
+    st = f.guide_stats()
+    f.close()
+    g.close()
+    ds.close()
+    return {"resolution": [width, height], "triangles": int(s.view().num_tris), "max_depth": int(p.max_depth),
+            "reference_spp": ref_spp, "reference_s": t_ref, "plain_spp": plain_spp, "plain_s": t_plain,
+            "plain_rmse": target, "guided_reached": reached, "guided_spp": done, "guided_s": spent,
+            "guided_rmse": last, "time_ratio": spent / t_plain if reached else None,
+            "adam_steps": st["adam_steps"], "training_samples": st["training_samples"],
+            "batch": batch, "train_every": every}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -366,6 +443,13 @@ def main():
     ctx = lf.Context(local)
     if args.engine_slots or args.shade_cap:
         ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap)
+    if args.workload == "c4":
+        r = run_guiding(ctx, 1280, 720, 4096)
+        if rank == 0:
+            print(json.dumps({"metric": "c4 guided / plain time to the plain 1024-spp error", "value": r["time_ratio"],
+                              "unit": "ratio", "higher_is_better": False, "detail": r}), flush=True)
+        ctx.close()
+        return
     if args.workload == "c5":
         r = run_serving(ctx, args.jobs or 48)
         if rank == 0:
@@ -374,7 +458,8 @@ def main():
         ctx.close()
         return
     if args.workload != "microbench":
-        r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags)
+        r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags,
+                         tune=args.autotune)
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)
@@ -453,7 +538,13 @@ def main():
         if not args.no_extras:
             for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8)):
                 try:
-                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags)
+                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags, tune=(w == "c3_1m"))
+                except Exception as e:  # reported, not fatal for the headline
+                    extra[w] = {"error": str(e)}
+            for w, fn in (("c4_guiding_640x360", lambda: run_guiding(ctx, 640, 360, 4096)),
+                          ("c5_serving_16_jobs", lambda: run_serving(ctx, 16, max_spp=64))):
+                try:
+                    extra[w] = fn()
                 except Exception as e:  # reported, not fatal for the headline
                     extra[w] = {"error": str(e)}
         extra.update({"scene_build_s": t_build, "scene_generate_s": t_gen, "hit_fraction": float((hits["prim"] >= 0).mean()),

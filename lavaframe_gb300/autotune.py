@@ -1,0 +1,81 @@
+"""Autotuner of the path engine (no reference counterpart).
+
+Chooses the engine's pool size (paths in flight), the block sizes of its extend and shadow
+kernels and the register cap of its shade kernel by timing short renders of the workload
+itself on the GPU, one knob at a time (coordinate descent from the current setting). The
+result is applied to the context and can be cached in a JSON file keyed by the workload
+signature (resolution, samples, depth, triangles).
+"""
+from __future__ import annotations
+
+import json
+import time
+from pathlib import Path
+
+CANDIDATES = {
+    "slots": [1 << 21, 1 << 22, 1 << 23, 1 << 24],
+    "shade_threads_per_sm": [0, 512, 768],
+    "block_extend": [64, 128, 256],
+    "block_shadow": [64, 128, 256],
+}
+DEFAULT = {"slots": 1 << 23, "shade_threads_per_sm": 768, "block_extend": 128, "block_shadow": 128}
+
+
+def _signature(params, spp, triangles):
+    return f"{params.width}x{params.height}:spp{spp}:depth{params.max_depth}:tris{triangles}"
+
+
+def _apply(ctx, cfg):
+    ctx.configure_engine(slots=cfg["slots"], block_extend=cfg["block_extend"], block_shade=128,
+                         block_shadow=cfg["block_shadow"], shade_threads_per_sm=cfg["shade_threads_per_sm"])
+
+
+def _time_render(ctx, device_scene, params, spp, repeats):
+    import lavaframe_gb300 as lf
+
+    f = lf.Frame(ctx, device_scene, params)
+    try:
+        f.render(0, 1)
+        f.sync()
+        best = float("inf")
+        for r in range(repeats):
+            f.reset()
+            t0 = time.perf_counter()
+            f.render(1 + r * spp, spp)
+            f.sync()
+            best = min(best, time.perf_counter() - t0)
+    finally:
+        f.close()
+    return best
+
+
+def tune(ctx, device_scene, params, spp=4, repeats=2, triangles=0, cache: str | Path | None = None):
+    """Tunes the engine of `ctx` for rendering `spp` samples of `params` on `device_scene` and
+    applies the best setting. Returns {"config", "seconds", "trials", "cached"}."""
+    key = _signature(params, spp, triangles)
+    store = {}
+    if cache is not None and Path(cache).exists():
+        store = json.loads(Path(cache).read_text())
+        if key in store:
+            _apply(ctx, store[key]["config"])
+            return dict(store[key], cached=True)
+    cfg = dict(DEFAULT)
+    _apply(ctx, cfg)
+    best = _time_render(ctx, device_scene, params, spp, repeats)
+    trials = [{"config": dict(cfg), "seconds": best}]
+    for knob, values in CANDIDATES.items():
+        for v in values:
+            if v == cfg[knob]:
+                continue
+            trial = dict(cfg, **{knob: v})
+            _apply(ctx, trial)
+            t = _time_render(ctx, device_scene, params, spp, repeats)
+            trials.append({"config": trial, "seconds": t})
+            if t < best:
+                best, cfg = t, trial
+    _apply(ctx, cfg)
+    result = {"config": cfg, "seconds": best, "trials": trials}
+    if cache is not None:
+        store[key] = {"config": cfg, "seconds": best}
+        Path(cache).write_text(json.dumps(store, indent=1))
+    return dict(result, cached=False)

@@ -76,11 +76,13 @@ __global__ void engine_init_kernel(EngineBuffers b)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
     {
         b.ps.info[i] = make_int4(0, 0, 0, -1);
-        b.done[0][i] = i;
+        b.freeList[i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
-        b.ctl->doneCount[0] = b.cap;
+        b.ctl->freeCount = b.cap;
+        b.ctl->taken = 0;
+        b.ctl->doneCount[0] = 0;
         b.ctl->doneCount[1] = 0;
         b.ctl->active = 0;
         b.ctl->count[0] = 0;
@@ -92,8 +94,7 @@ __global__ void engine_init_kernel(EngineBuffers b)
 __global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, unsigned long long numPasses)
 {
     EngineCtl* c = b.ctl;
-    unsigned long long next = c->next < c->total ? c->next : c->total;
-    c->next = next;
+    const unsigned long long next = c->next;
     c->total = total;
     c->numPasses = numPasses;
     unsigned long long lo = c->passLo;
@@ -106,102 +107,91 @@ __global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, 
     c->passLo = lo;
 }
 
+// After finish and refill: take the refilled slots off the free list and the ids off the
+// pool of unissued paths, and clear the lists the rest of the step refills.
 __global__ void engine_reset_kernel(EngineCtl* c, int parity)
 {
+    c->freeCount -= c->taken;
+    c->next += (unsigned long long)c->taken;
+    c->active += c->taken;
+    c->taken = 0;
     c->doneCount[parity] = 0;
     c->shadowCount = 0;
     c->count[parity ^ 1] = 0;
 }
 
-// ------------------------------------------------------------------ finish
-// Writes out the radiance of every finished path, then gives each freed slot the next
-// unissued path id (camera ray of renderer.glsl:27-62) and queues it for extension. Slots
-// left without work wait on the other done list for a later append.
-template <bool kOne>
-__global__ void engine_finish_kernel(EngineBuffers b, EngineJob one, int parity)
+// ------------------------------------------------------------------ finish / refill
+// Writes out the radiance of every path that finished in the previous step (counting pass
+// completions) and returns its slot to the free list.
+__global__ void engine_finish_kernel(EngineBuffers b, int parity)
 {
     __shared__ int smem[33];
-    __shared__ unsigned long long sFirst;
     __shared__ DoneTable table;
     EngineCtl* ctl = b.ctl;
     const int n = ctl->doneCount[parity];
     const int* done = b.done[parity];
-    const unsigned long long total = ctl->total;
-    const unsigned long long plo = ctl->passLo, phi = ctl->numPasses;
-    const bool work = ctl->next < total;
-    int* q = b.queue[parity];
-    int* qc = &ctl->count[parity];
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    // block-uniform loop: block_push synchronises the block
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)   // block-uniform
     {
         const int i = base + threadIdx.x;
         const int slot = i < n ? done[i] : -1;
         int ring = -1;
         if (slot >= 0)
         {
-            const int w = reinterpret_cast<const int*>(b.ps.info)[4 * slot + 3];
-            if (w >= 0)
-            {
-                ring = ring_of(w);
-                const int local = reinterpret_cast<const int*>(b.ps.info)[4 * slot];
-                b.passes[ring].radiance[local] = b.ps.L[slot];
-            }
+            int* info = reinterpret_cast<int*>(b.ps.info) + 4 * slot;
+            ring = ring_of(info[3]);
+            b.passes[ring].radiance[info[0]] = b.ps.L[slot];
+            info[3] = -1;
         }
         count_done_block(ring, b.passDone, table);
+        block_push(slot >= 0, slot, b.freeList, &ctl->freeCount, b.cap, b.status, smem);
+        const int written = __popc(__ballot_sync(kFull, ring >= 0));
+        if (lane == 0 && written) atomicSub(&ctl->active, written);
+    }
+}
 
-        bool started = false, push = false;
-        if (work)
+// Starts min(free slots, unissued ids) new paths: the k-th one takes id next + k and the k-th
+// slot from the top of the free list, gets its camera ray (renderer.glsl:27-62) and is queued
+// for extension (a depth-0 job's paths go straight to the done list with zero radiance).
+template <bool kOne>
+__global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    __shared__ int smem[33];
+    EngineCtl* ctl = b.ctl;
+    const unsigned long long next = ctl->next, total = ctl->total;
+    const int freeCount = ctl->freeCount;
+    const unsigned long long left = next < total ? total - next : 0ull;
+    const int m = (int)((unsigned long long)freeCount < left ? (unsigned long long)freeCount : left);
+    if (m <= 0) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->taken = m;
+    const unsigned long long plo = ctl->passLo, phi = ctl->numPasses;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < m; base += stride)   // block-uniform
+    {
+        const int k = base + threadIdx.x;
+        int slot = -1;
+        bool run = false;
+        if (k < m)
         {
-            // one id range per block: warp offsets in smem, one atomic on `next`
-            const unsigned need = __ballot_sync(kFull, slot >= 0);
-            const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-            if (lane == 0) smem[warp] = __popc(need);
-            __syncthreads();
-            if (threadIdx.x == 0)
-            {
-                int tot = 0;
-                for (int w = 0; w < nw; ++w)
-                {
-                    const int c = smem[w];
-                    smem[w] = tot;
-                    tot += c;
-                }
-                sFirst = tot ? atomicAdd(&ctl->next, (unsigned long long)tot) : 0ull;
-            }
-            __syncthreads();
-            const unsigned long long first = sFirst + (unsigned long long)smem[warp];
-            __syncthreads();
-            if (slot >= 0)
-            {
-                const unsigned long long id = first + __popc(need & ((1u << lane) - 1u));
-                if (id < total)
-                {
-                    const unsigned long long g = find_pass(b.passes, id, plo, phi);
-                    const int r = (int)(g & (kPassRing - 1));
-                    const EnginePass& Q = b.passes[r];
-                    const Params& P = kOne ? one.P : b.jobs[Q.job].P;
-                    const int local = (int)(id - Q.pathBase);   // passes hold < 2^31 paths
-                    const int visPix = Q.visW * Q.visH;
-                    const int s = local / visPix;
-                    const int lp = local - s * visPix;
-                    const int ly = lp / Q.visW, lx = lp - ly * Q.visW;
-                    b.ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    b.ps.info[slot] = make_int4(local, 0, 0, r | (Q.job << kPassRingBits));
-                    gen_path(P, Q.tileX, Q.tileY, Q.tileOrdinal, Q.firstSample + s, lx, ly, b.ps, slot);
-                    started = true;
-                    push = P.maxDepth > 0;   // depth 0: the path ends with zero radiance
-                }
-            }
+            slot = b.freeList[freeCount - 1 - k];
+            const unsigned long long id = next + (unsigned long long)k;
+            const unsigned long long g = find_pass(b.passes, id, plo, phi);
+            const int r = (int)(g & (kPassRing - 1));
+            const EnginePass& Q = b.passes[r];
+            const Params& P = kOne ? one.P : b.jobs[Q.job].P;
+            const int local = (int)(id - Q.pathBase);   // passes hold < 2^31 paths
+            const int visPix = Q.visW * Q.visH;
+            const int s = local / visPix;
+            const int lp = local - s * visPix;
+            const int ly = lp / Q.visW, lx = lp - ly * Q.visW;
+            b.ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+            b.ps.info[slot] = make_int4(local, 0, 0, r | (Q.job << kPassRingBits));
+            gen_path(P, Q.tileX, Q.tileY, Q.tileOrdinal, Q.firstSample + s, lx, ly, b.ps, slot);
+            run = P.maxDepth > 0;
         }
-        if (slot >= 0 && !started && ring >= 0)
-            reinterpret_cast<int*>(b.ps.info)[4 * slot + 3] = -1;   // idle until the next append
-        block_push(push, slot, q, qc, b.cap, b.status, smem);
-        block_push(slot >= 0 && !push, slot, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
-        // active += started - written out, one atomic per warp
-        const int delta = __popc(__ballot_sync(kFull, started)) - __popc(__ballot_sync(kFull, ring >= 0));
-        if (lane == 0 && delta != 0) atomicAdd(&ctl->active, delta);
+        block_push(run, slot, b.queue[parity], &ctl->count[parity], b.cap, b.status, smem);
+        block_push(slot >= 0 && !run, slot, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
     }
 }
 
@@ -377,7 +367,8 @@ template <bool kOne>
 void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t st)
 {
     const int BF = 256;
-    engine_finish_kernel<kOne><<<full_grid((const void*)engine_finish_kernel<kOne>, BF, b.cap), BF, 0, st>>>(b, one,
+    engine_finish_kernel<<<full_grid((const void*)engine_finish_kernel, BF, b.cap), BF, 0, st>>>(b, parity);
+    engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, BF, b.cap), BF, 0, st>>>(b, one,
                                                                                                           parity);
     engine_reset_kernel<<<1, 1, 0, st>>>(b.ctl, parity);
     const int be = b.blockExtend > 0 ? b.blockExtend : 128;

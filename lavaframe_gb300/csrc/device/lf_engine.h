@@ -10,9 +10,9 @@
 // image sums are the ones of the per-batch pipeline, bit for bit.
 //
 // One engine step with parity k (graph-captured, two steps per graph so the parity returns):
-//   finish   done[k]: write out finished paths, count pass completions, start new paths
-//            (-> queue[k]); slots left without work go to done[k^1]
-//   reset    clear done[k], the shadow queue and queue[k^1]
+//   finish   done[k]: write out finished paths, count pass completions, free their slots
+//   refill   start new paths in free slots while unissued ids remain (-> queue[k])
+//   reset    commit the refill, clear done[k], the shadow queue and queue[k^1]
 //   extend   closest hit of every queued path
 //   shade    one PathTrace bounce; survivors -> queue[k^1], finished -> done[k^1]
 //   shadow   next-event visibility
@@ -45,7 +45,7 @@ struct EnginePass
 
 struct EngineCtl
 {
-    unsigned long long next;       // next global path id to issue (may overshoot total)
+    unsigned long long next;       // next global path id to issue
     unsigned long long total;      // ids available
     unsigned long long passLo;     // first pass that may still have unissued ids
     unsigned long long numPasses;  // passes submitted
@@ -53,6 +53,8 @@ struct EngineCtl
     int shadowCount;
     int doneCount[2];              // done-list sizes
     int active;                    // paths started and not yet written out
+    int freeCount;                 // slots on the free list
+    int taken;                     // slots the current step's refill started
 };
 
 struct EngineBuffers
@@ -60,7 +62,8 @@ struct EngineBuffers
     PathSoA ps;                  // info: x local path id, y depth, z last material, w ring | job << 14
     int* queue[2];
     ShadowRec* shadow;
-    int* done[2];                // slots whose path finished, or that are idle
+    int* done[2];                // slots whose path finished
+    int* freeList;               // slots without a path (a stack)
     EngineCtl* ctl;
     const EngineJob* jobs;
     const EnginePass* passes;    // ring of kPassRing

@@ -11,7 +11,8 @@ namespace lfrt
 {
 namespace
 {
-constexpr int kDefaultSlots = 1 << 21;
+constexpr int kDefaultSlots = 1 << 23;      // ~2 GB of path state: enough rays in flight for 152 SMs
+constexpr int kDefaultShadeCap = 768;       // shade kernel register cap (threads per SM)
 constexpr int kMaxJobs = 4096;
 constexpr size_t kRunRadianceBytes = size_t(2) << 30;   // radiance buffers of one frame run
 
@@ -51,6 +52,7 @@ lf_status alloc_pool(EngineHost* e, int slots)
     A(&b.queue[1], slots);
     A(&b.done[0], slots);
     A(&b.done[1], slots);
+    A(&b.freeList, slots);
     A(&b.shadow, slots);
     if (err != cudaSuccess)
     {
@@ -98,6 +100,7 @@ lf_status engine_get(lf_ctx* c, EngineHost** out)
     e->b.passes = passes;
     e->b.status = c->d_status;
     e->b.ctr = e->ownCtr;
+    e->b.shadeThreadsPerSm = kDefaultShadeCap;
     e->jobUsed.assign(kMaxJobs, 0);
     e->jobGen.assign(kMaxJobs, 0);
     // pass radiance buffers come from the stream-ordered pool; keep up to 8 GB of it cached

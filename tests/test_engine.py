@@ -13,7 +13,8 @@ from tests import scenes
 
 pytestmark = pytest.mark.gpu
 
-DEFAULT_SLOTS = 1 << 21
+DEFAULT_SLOTS = 1 << 23
+DEFAULT_SHADE_CAP = 768
 
 
 def icospheres():
@@ -71,7 +72,8 @@ def test_small_pool_regenerates_and_matches_oracle(ctx):
         assert same_bits(got["paths"], ref_paths)
         assert same_bits(got["accum"], ref_acc)
     finally:
-        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0)
+        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
+                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
 
 
 @pytest.mark.parametrize("blocks", [(64, 256, 96), (256, 64, 512)])
@@ -82,7 +84,7 @@ def test_engine_block_sizes_do_not_change_results(ctx, blocks):
         ctx.configure_engine(0, *blocks)
         got, _ = render(ctx, s, 2)
     finally:
-        ctx.configure_engine(0, 0, 0, 0)
+        ctx.configure_engine(0, 0, 0, 0, DEFAULT_SHADE_CAP)
     assert same_bits(got["paths"], base["paths"])
     assert same_bits(got["accum"], base["accum"])
 
@@ -113,3 +115,23 @@ def test_frames_of_two_scenes_alternate(ctx):
     assert same_bits(fb.accum(), rb)
     for h in (fa, fb, da, db):
         h.close()
+
+
+def test_autotuner_picks_a_setting_and_results_stay_exact(ctx, tmp_path):
+    from lavaframe_gb300 import autotune
+
+    s = scenes.build("cornell")
+    base, p = render(ctx, s, 2)
+    ds = ctx.upload(s)
+    try:
+        cache = tmp_path / "tune.json"
+        r = autotune.tune(ctx, ds, p, spp=2, repeats=1, triangles=int(s.view().num_tris), cache=cache)
+        assert set(r["config"]) == set(autotune.DEFAULT) and len(r["trials"]) >= 10 and not r["cached"]
+        again = autotune.tune(ctx, ds, p, spp=2, repeats=1, triangles=int(s.view().num_tris), cache=cache)
+        assert again["cached"] and again["config"] == r["config"]
+        got, _ = render(ctx, s, 2)
+    finally:
+        ds.close()
+        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
+                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
+    assert same_bits(got["paths"], base["paths"])
