@@ -47,9 +47,11 @@ def parse():
     ap.add_argument("--spp-batch", type=int, default=0, help="samples per wavefront batch of the render workloads")
     ap.add_argument("--frame-flags", type=int, default=0, help="lf_frame flags of the render workloads (8 = per-batch)")
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
-    ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (0/512/768)")
+    ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768; 0 = 768)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
+    ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
+    ap.add_argument("--c4-ref-spp", type=int, default=4096, help="guiding workload reference samples")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
@@ -442,9 +444,10 @@ def main():
     b.build_oracle()
     ctx = lf.Context(local)
     if args.engine_slots or args.shade_cap:
-        ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap)
+        ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 768)
     if args.workload == "c4":
-        r = run_guiding(ctx, 1280, 720, 4096)
+        cw, ch = (int(x) for x in args.c4_size.split("x"))
+        r = run_guiding(ctx, cw, ch, args.c4_ref_spp)
         if rank == 0:
             print(json.dumps({"metric": "c4 guided / plain time to the plain 1024-spp error", "value": r["time_ratio"],
                               "unit": "ratio", "higher_is_better": False, "detail": r}), flush=True)

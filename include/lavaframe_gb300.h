@@ -179,6 +179,11 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* view);
 lf_status lf_scene_release(lf_scene* sc);
 /* Culling margins of the traversal (relative, absolute); rel < 0 turns culling off. */
 lf_status lf_scene_set_culling(lf_scene* sc, float rel, float abs_margin);
+/* Traversal of the scene's queries and renders: 1 = the 4-wide tree collapsed from the
+ * reference BVH (default), 0 = the reference's binary tree. Both return the reference's
+ * hits: the wide tree tests the same leaves and resolves equal distances by the reference's
+ * depth-first order. */
+lf_status lf_scene_set_traversal(lf_scene* sc, int32_t wide);
 size_t lf_scene_device_bytes(const lf_scene* sc);
 
 /* ------------------------------------------------------------------ ray queries

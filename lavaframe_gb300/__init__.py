@@ -70,6 +70,7 @@ _SIG = {
     "lf_scene_update_instances": (C.c_int, [_P, _P]),
     "lf_scene_release": (C.c_int, [_P]),
     "lf_scene_set_culling": (C.c_int, [_P, C.c_float, C.c_float]),
+    "lf_scene_set_traversal": (C.c_int, [_P, C.c_int32]),
     "lf_scene_device_bytes": (C.c_size_t, [_P]),
     "lf_trace_closest": (C.c_int, [_P, _P, _F, C.c_int64, _P, C.c_uint32]),
     "lf_trace_any": (C.c_int, [_P, _P, _F, C.c_int64, _P, C.c_uint32]),
@@ -395,6 +396,10 @@ class DeviceScene:
         self.ctx = ctx
         self.h = _P()
         ctx._c(lib().lf_scene_upload(ctx.h, C.byref(view), C.byref(self.h)))
+
+    def set_traversal(self, wide):
+        """1: 4-wide tree (default); 0: the reference's binary tree."""
+        self.ctx._c(lib().lf_scene_set_traversal(self.h, 1 if wide else 0))
 
     def set_culling(self, rel, abs_margin=0.0):
         self.ctx._c(lib().lf_scene_set_culling(self.h, rel, abs_margin))

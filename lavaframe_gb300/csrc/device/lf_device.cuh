@@ -51,6 +51,14 @@ struct DevLight
     float pad[3];
 };
 
+// 4-wide nodes collapsed from the reference's binary tree (see traverse_wide): per node
+// 2 * kWide float4 = [min x | max x | min y | max y | min z | max z | child codes | child
+// reference-node indices], kWide values per group; unused slots have code kWideEmpty.
+constexpr int kWide = 4;
+constexpr int kWideF4 = 2 * kWide;
+constexpr int kWideEmpty = (int)0x80000002;
+constexpr int kWideStack = 96;
+
 struct DevScene
 {
     const float4* nodes;        // 4 float4 per inner node
@@ -62,6 +70,12 @@ struct DevScene
     int numNodes, numTris, numInstances;
     float cullRel;              // relative culling margin, < 0 disables culling
     float cullAbs;              // absolute culling margin (a few ulps of the scene extent)
+    // wide traversal (null wnodes or wideOn == 0: binary traversal everywhere)
+    const float4* wnodes;       // kWideF4 float4 per wide node
+    int wroot;                  // instance-level root code in the wide tree
+    int wideOn;
+    const float* refNodes;      // the reference's 36-byte nodes, for tie resolution
+    const int* refParent;       // parent of every reference node, -1 at roots
 };
 
 struct TraceStats
@@ -353,6 +367,301 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
     return err;
 }
 
+// ------------------------------------------------------------------ wide traversal
+// The 4-wide tree is the reference's binary tree with intermediate levels collapsed: its leaves
+// are the reference's leaves and every child box is the box of a reference node. For rays
+// whose inverse direction is regular (box_hit_fast), a slab test is monotone in the box, so a
+// node's box passes only if every ancestor's box passes: the triangles tested are exactly the
+// ones of the leaves whose boxes pass - the reference's set, in a different order. The order
+// only matters for hits at the same distance; those are resolved by the reference's
+// depth-first order (ref_first). Rays with a degenerate direction take the binary traversal.
+
+// True when the reference's depth-first traversal of the tree holding reference nodes a and b
+// reaches a before b: at their lowest common ancestor it descends into the child whose box
+// value is smaller (ties left, closest_hit.glsl:172-187), exact box test with the level's ray.
+static __device__ __noinline__ bool ref_first(const DevScene& S, int a, int b, v3 o, v3 invd)
+{
+    int da = 0, db = 0;
+    for (int x = a; S.refParent[x] >= 0 && da < 1024; x = S.refParent[x]) ++da;
+    for (int x = b; S.refParent[x] >= 0 && db < 1024; x = S.refParent[x]) ++db;
+    for (; da > db; --da) a = S.refParent[a];
+    for (; db > da; --db) b = S.refParent[b];
+    for (int g = 0; g < 1024 && a != b && S.refParent[a] != S.refParent[b]; ++g)
+    {
+        a = S.refParent[a];
+        b = S.refParent[b];
+    }
+    if (a == b || S.refParent[a] < 0) return false;
+    const float* P = S.refNodes + (size_t)S.refParent[a] * 9;
+    const int l = (int)P[6], r = (int)P[7];
+    const float* Ln = S.refNodes + (size_t)l * 9;
+    const float* Rn = S.refNodes + (size_t)r * 9;
+    float e;
+    const float hL = box_hit(Ln[0], Ln[1], Ln[2], Ln[3], Ln[4], Ln[5], o, invd, &e);
+    const float hR = box_hit(Rn[0], Rn[1], Rn[2], Rn[3], Rn[4], Rn[5], o, invd, &e);
+    const int nearC = (hL > 0.f && hR > 0.f) ? (hL > hR ? r : l) : (hL > 0.f ? l : r);
+    return a == nearC;
+}
+
+// Binary traversal of one mesh level (the reference's order and exact box test) for an
+// object-space ray whose direction is degenerate. Updates t / out like traverse; a hit at the
+// same distance as the best hit of another instance is resolved by the instance tree's order
+// (world ray wo / winvd, reference nodes of the two instances' leaves).
+template <bool kAny>
+__device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, int inst, v3 ro, v3 rd, float* tio,
+                                             Hit* out, bool* anyHit, v3 wo, v3 winvd, int instRef, int bestInstRef)
+{
+    int stack[kStackSize];
+    int sp = 0;
+    const int kEmptyB = (int)0x80000001;
+    const v3 invd = 1.0f / rd;
+    const bool cull = S.cullRel >= 0.f;
+    float t = *tio;
+    int code = rootCode;
+    uint32_t err = 0;
+    for (int steps = 0;; )
+    {
+        if (++steps > kMaxTraversalSteps) { err |= LF_DEVERR_STEPS; break; }
+        if (code == kEmptyB)
+        {
+            if (sp == 0) break;
+            code = stack[--sp];
+            continue;
+        }
+        if (code < 0)
+        {
+            const int payload = ~code;
+            const int first = payload >> 2, cnt = payload & 3;
+            for (int i = 0; i < cnt; ++i)
+            {
+                float u, v;
+                const float tt = tri_hit(S.tris + (size_t)(first + i) * 3, ro, rd, &u, &v);
+                const bool tie = !kAny && tt == t && tt >= 0.f && out->prim >= 0 && out->inst != inst &&
+                                 ref_first(S, instRef, bestInstRef, wo, winvd);
+                if ((tt >= 0.f && tt < t) || tie)
+                {
+                    t = tt;
+                    out->prim = first + i;
+                    out->inst = inst;
+                    out->light = -1;
+                    if (kAny)
+                    {
+                        *anyHit = true;
+                        *tio = t;
+                        return err;
+                    }
+                }
+            }
+            code = kEmptyB;
+            continue;
+        }
+        const float4* rec = S.nodes + (size_t)code * 4;
+        const float4 f0 = ldg4(rec + 0), f1 = ldg4(rec + 1), f2 = ldg4(rec + 2), f3 = ldg4(rec + 3);
+        float eL, eR;
+        float hL = box_hit_exact(f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, ro, invd, &eL);
+        float hR = box_hit_exact(f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, ro, invd, &eR);
+        if (cull)
+        {
+            const float lim = t + t * S.cullRel + S.cullAbs;
+            if (eL > lim) hL = -1.0f;
+            if (eR > lim) hR = -1.0f;
+        }
+        const int cL = __float_as_int(f3.x), cR = __float_as_int(f3.y);
+        if (hL > 0.f && hR > 0.f)
+        {
+            int nearC = cL, farC = cR;
+            if (hL > hR) { nearC = cR; farC = cL; }
+            if (sp >= kStackCap) { err |= LF_DEVERR_STACK; break; }
+            stack[sp++] = farC;
+            code = nearC;
+        }
+        else if (hL > 0.f)
+            code = cL;
+        else if (hR > 0.f)
+            code = cR;
+        else
+            code = kEmptyB;
+    }
+    *tio = t;
+    return err;
+}
+
+template <bool kAny>
+__device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d, float* tBest, Hit* out)
+{
+    bool fast;
+    const v3 winvd = inv_dir(d, &fast);
+    if (!fast) return traverse<kAny, false>(S, o, d, tBest, out, nullptr);
+    const int kBlasEnd = (int)0x80000000;
+    const int kEmpty = (int)0x80000001;
+    int2 stack[kWideStack];   // (code, reference node)
+    int sp = 0;
+    int code = S.wroot, cref = -1;
+    bool meshLevel = false;
+    int curInst = -1, curInstRef = -1;
+    int bestLeafRef = -1, bestInstRef = -1;
+    v3 ro = o, rd = d, invd = winvd;
+    uint32_t err = 0;
+    const bool cull = S.cullRel >= 0.f;
+    float t = *tBest;
+    int steps = 0;
+    while (true)
+    {
+        if (++steps > kMaxTraversalSteps) { err |= LF_DEVERR_STEPS; break; }
+        if (code == kEmpty)
+        {
+            if (sp == 0) break;
+            const int2 e = stack[--sp];
+            code = e.x;
+            cref = e.y;
+            if (code == kBlasEnd)
+            {
+                meshLevel = false;
+                ro = o;
+                rd = d;
+                invd = winvd;
+                code = kEmpty;
+            }
+            continue;
+        }
+        if (code < 0)
+        {
+            const int payload = ~code;
+            if (meshLevel)
+            {
+                const int first = payload >> 2, cnt = payload & 3;
+                for (int i = 0; i < cnt; ++i)
+                {
+                    float u, v;
+                    const int prim = first + i;
+                    const float tt = tri_hit(S.tris + (size_t)prim * 3, ro, rd, &u, &v);
+                    if (tt >= 0.f && tt <= t)
+                    {
+                        bool take = tt < t;
+                        if (!take && !kAny && out->prim >= 0)
+                        {
+                            // equal distance: the reference keeps the one it reaches first
+                            if (curInst == out->inst)
+                                take = cref == bestLeafRef ? prim < out->prim : ref_first(S, cref, bestLeafRef, ro, invd);
+                            else
+                                take = ref_first(S, curInstRef, bestInstRef, o, winvd);
+                        }
+                        if (take)
+                        {
+                            t = tt;
+                            out->prim = prim;
+                            out->inst = curInst;
+                            out->light = -1;
+                            bestLeafRef = cref;
+                            bestInstRef = curInstRef;
+                            if (kAny)
+                            {
+                                *tBest = t;
+                                return err;
+                            }
+                        }
+                    }
+                }
+                code = kEmpty;
+            }
+            else
+            {
+                const int inst = payload;
+                const float4* ir = S.instances + (size_t)inst * 4;
+                float m[12];
+                int root, mat;
+                load_instance(ir, m, &root, &mat);
+                const float4 e3 = ldg4(ir + 3);
+                const v3 iro = xform(m, o, 1.0f), ird = xform(m, d, 0.0f);
+                bool ofast;
+                const v3 iinvd = inv_dir(ird, &ofast);
+                if (!ofast)
+                {
+                    const int before = out->prim;
+                    const int beforeInst = out->inst;
+                    bool anyHit = false;
+                    err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd, cref, bestInstRef);
+                    if (kAny && anyHit)
+                    {
+                        *tBest = t;
+                        return err;
+                    }
+                    if (out->prim != before || out->inst != beforeInst)
+                    {
+                        bestLeafRef = -1;   // no later hit of this instance can tie with it
+                        bestInstRef = cref;
+                    }
+                    code = kEmpty;
+                    continue;
+                }
+                if (sp >= kWideStack)
+                {
+                    err |= LF_DEVERR_STACK;
+                    break;
+                }
+                stack[sp++] = make_int2(kBlasEnd, -1);
+                ro = iro;
+                rd = ird;
+                invd = iinvd;
+                meshLevel = true;
+                curInst = inst;
+                curInstRef = cref;
+                code = __float_as_int(e3.z);
+                cref = __float_as_int(e3.w);
+            }
+            continue;
+        }
+        const float4* rec = S.wnodes + (size_t)code * kWideF4;
+        const float4 mnx = ldg4(rec + 0), mxx = ldg4(rec + 1), mny = ldg4(rec + 2), mxy = ldg4(rec + 3);
+        const float4 mnz = ldg4(rec + 4), mxz = ldg4(rec + 5), cc = ldg4(rec + 6), rr = ldg4(rec + 7);
+        const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
+        const float bx0[4] = {mnx.x, mnx.y, mnx.z, mnx.w}, bx1[4] = {mxx.x, mxx.y, mxx.z, mxx.w};
+        const float by0[4] = {mny.x, mny.y, mny.z, mny.w}, by1[4] = {mxy.x, mxy.y, mxy.z, mxy.w};
+        const float bz0[4] = {mnz.x, mnz.y, mnz.z, mnz.w}, bz1[4] = {mxz.x, mxz.y, mxz.z, mxz.w};
+        const int cds[4] = {__float_as_int(cc.x), __float_as_int(cc.y), __float_as_int(cc.z), __float_as_int(cc.w)};
+        const int rfs[4] = {__float_as_int(rr.x), __float_as_int(rr.y), __float_as_int(rr.z), __float_as_int(rr.w)};
+        float hd[4];
+        int hc[4], hr[4];
+        int nh = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+            float e;
+            const float h = box_hit_fast(bx0[j], by0[j], bz0[j], bx1[j], by1[j], bz1[j], ro, invd, &e);
+            if (cds[j] != kWideEmpty && h > 0.f && e <= lim)
+            {
+                // insertion by entry distance, nearest first
+                int k = nh++;
+                while (k > 0 && hd[k - 1] > e)
+                {
+                    hd[k] = hd[k - 1];
+                    hc[k] = hc[k - 1];
+                    hr[k] = hr[k - 1];
+                    --k;
+                }
+                hd[k] = e;
+                hc[k] = cds[j];
+                hr[k] = rfs[j];
+            }
+        }
+        if (nh == 0)
+        {
+            code = kEmpty;
+            continue;
+        }
+        if (sp + nh - 1 > kWideStack)
+        {
+            err |= LF_DEVERR_STACK;
+            break;
+        }
+        for (int k = nh - 1; k >= 1; --k) stack[sp++] = make_int2(hc[k], hr[k]);
+        code = hc[0];
+        cref = hr[0];
+    }
+    *tBest = t;
+    return err;
+}
+
 // Closest hit: analytic lights first (closest_hit.glsl:13-67), then the BVH.
 template <bool kStats>
 __device__ __forceinline__ uint32_t closest_hit(const DevScene& S, v3 o, v3 d, float tInit, bool useLights,
@@ -384,7 +693,8 @@ __device__ __forceinline__ uint32_t closest_hit(const DevScene& S, v3 o, v3 d, f
             }
         }
     }
-    uint32_t err = traverse<false, kStats>(S, o, d, &t, out, st);
+    uint32_t err = (!kStats && S.wnodes && S.wideOn) ? traverse_wide<false>(S, o, d, &t, out)
+                                                      : traverse<false, kStats>(S, o, d, &t, out, st);
     out->t = t;
     return err;
 }
@@ -416,7 +726,8 @@ __device__ __forceinline__ uint32_t any_hit(const DevScene& S, v3 o, v3 d, float
         }
     }
     float t = maxDist;
-    uint32_t err = traverse<true, kStats>(S, o, d, &t, out, st);
+    uint32_t err = (!kStats && S.wnodes && S.wideOn) ? traverse_wide<true>(S, o, d, &t, out)
+                                                     : traverse<true, kStats>(S, o, d, &t, out, st);
     *occluded = out->prim >= 0;
     out->t = *occluded ? t : kInfinity;
     return err;

@@ -65,6 +65,10 @@ struct lf_scene
     DevMaterial* d_materials = nullptr;
     int numMaterials = 0;
     std::vector<int> meshNodeMap;   // reference index -> device record (mesh levels), -1 otherwise
+    float4* d_wide = nullptr;       // wide tree
+    size_t wideCapacity = 0;        // wide records allocated
+    float* d_refNodes = nullptr;    // the reference nodes (tie resolution)
+    int* d_parent = nullptr;
     float boundsLo[3] = {0, 0, 0}, boundsHi[3] = {0, 0, 0};   // instance-level root box
 };
 

@@ -231,6 +231,188 @@ lf_status encode_level(lf_ctx* c, const RefNode* nodes, int numNodes, int start,
     return LF_OK;
 }
 
+// ------------------------------------------------------------------ wide (4-way) tree
+// Every wide node holds up to four reference nodes as children: starting from a reference
+// inner node's two children, the inner child with the largest box surface area is replaced by
+// its two children until four children are reached or only leaves remain. Leaves keep the
+// binary encoding's codes; every child slot carries the reference node's own box and index.
+struct WideBuilder
+{
+    const RefNode* nodes = nullptr;
+    int numNodes = 0, numTris = 0, numInstances = 0;
+    std::vector<float4> recs;
+    std::vector<int> map;   // reference inner node -> wide record it heads
+};
+
+bool ref_leaf_code(const RefNode& n, bool meshLevel, int numTris, int numInstances, int* code)
+{
+    const int z = (int)n.lr[2];
+    if (meshLevel)
+    {
+        if (z <= 0) return false;
+        const int first = (int)n.lr[0], cnt = (int)n.lr[1];
+        if (first < 0 || cnt < 0 || cnt > 3 || first + cnt > numTris) return false;
+        *code = ~((first << 2) | cnt);
+    }
+    else
+    {
+        if (z >= 0) return false;
+        const int inst = -z - 1;
+        if (inst >= numInstances) return false;
+        *code = ~inst;
+    }
+    return true;
+}
+
+float box_area(const RefNode& n)
+{
+    const float dx = n.bmax[0] - n.bmin[0], dy = n.bmax[1] - n.bmin[1], dz = n.bmax[2] - n.bmin[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+lf_status wide_level(lf_ctx* c, WideBuilder& B, int start, bool meshLevel, int* rootCode)
+{
+    if (start < 0 || start >= B.numNodes) return fail(c, LF_ERR_INVALID, "node index out of range");
+    const RefNode& r = B.nodes[start];
+    if ((int)r.lr[2] != 0)
+    {
+        if (!ref_leaf_code(r, meshLevel, B.numTris, B.numInstances, rootCode))
+            return fail(c, LF_ERR_INVALID, "bad leaf node " + std::to_string(start));
+        return LF_OK;
+    }
+    if (B.map[start] >= 0)
+    {
+        *rootCode = B.map[start];
+        return LF_OK;
+    }
+    auto inner = [&](int i) { return (int)B.nodes[i].lr[2] == 0; };
+    B.map[start] = (int)(B.recs.size() / kWideF4);
+    B.recs.resize(B.recs.size() + kWideF4);
+    std::vector<int> stack{start};
+    while (!stack.empty())
+    {
+        const int ref = stack.back();
+        stack.pop_back();
+        const int rec = B.map[ref];
+        std::vector<int> kids{(int)B.nodes[ref].lr[0], (int)B.nodes[ref].lr[1]};
+        for (int k : kids)
+            if (k < 0 || k >= B.numNodes) return fail(c, LF_ERR_INVALID, "child index out of range");
+        while ((int)kids.size() < kWide)
+        {
+            int best = -1;
+            float area = -1.f;
+            for (int k = 0; k < (int)kids.size(); ++k)
+                if (inner(kids[k]) && box_area(B.nodes[kids[k]]) > area)
+                {
+                    area = box_area(B.nodes[kids[k]]);
+                    best = k;
+                }
+            if (best < 0) break;
+            const int x = kids[best];
+            const int xl = (int)B.nodes[x].lr[0], xr = (int)B.nodes[x].lr[1];
+            if (xl < 0 || xl >= B.numNodes || xr < 0 || xr >= B.numNodes)
+                return fail(c, LF_ERR_INVALID, "child index out of range");
+            kids[best] = xl;
+            kids.insert(kids.begin() + best + 1, xr);
+        }
+        float f[8][kWide];
+        for (int j = 0; j < kWide; ++j)
+        {
+            int code = kWideEmpty, refIdx = -1;
+            float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+            if (j < (int)kids.size())
+            {
+                const int k = kids[j];
+                const RefNode& n = B.nodes[k];
+                for (int a = 0; a < 3; ++a)
+                {
+                    lo[a] = n.bmin[a];
+                    hi[a] = n.bmax[a];
+                }
+                refIdx = k;
+                if (inner(k))
+                {
+                    if (B.map[k] >= 0) return fail(c, LF_ERR_INVALID, "node referenced twice: " + std::to_string(k));
+                    B.map[k] = (int)(B.recs.size() / kWideF4);
+                    B.recs.resize(B.recs.size() + kWideF4);
+                    code = B.map[k];
+                    stack.push_back(k);
+                }
+                else if (!ref_leaf_code(n, meshLevel, B.numTris, B.numInstances, &code))
+                    return fail(c, LF_ERR_INVALID, "bad leaf node " + std::to_string(k));
+            }
+            f[0][j] = lo[0];
+            f[1][j] = hi[0];
+            f[2][j] = lo[1];
+            f[3][j] = hi[1];
+            f[4][j] = lo[2];
+            f[5][j] = hi[2];
+            std::memcpy(&f[6][j], &code, 4);
+            std::memcpy(&f[7][j], &refIdx, 4);
+        }
+        float4* o = &B.recs[(size_t)rec * kWideF4];
+        for (int g = 0; g < 8; ++g) o[g] = make_float4(f[g][0], f[g][1], f[g][2], f[g][3]);
+    }
+    *rootCode = B.map[start];
+    return LF_OK;
+}
+
+// Wide tree of the whole scene (mesh levels first, then the instance level), the instance
+// records' wide root codes and mesh root reference nodes, and the reference parent array.
+lf_status encode_wide(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, std::vector<float4>& inst,
+                      std::vector<float4>& wrecs, std::vector<int>& parent, int* wroot)
+{
+    WideBuilder B;
+    B.nodes = nodes;
+    B.numNodes = v->num_nodes;
+    B.numTris = v->num_tris;
+    B.numInstances = v->num_instances;
+    B.map.assign(v->num_nodes, -1);
+    std::vector<int> instRoot(v->num_instances, -1);
+    std::vector<int> stack{v->top_level_index};
+    while (!stack.empty())
+    {
+        const int ref = stack.back();
+        stack.pop_back();
+        const RefNode& n = nodes[ref];
+        const int z = (int)n.lr[2];
+        if (z < 0)
+            instRoot[-z - 1] = (int)n.lr[0];
+        else if (z == 0)
+        {
+            stack.push_back((int)n.lr[1]);
+            stack.push_back((int)n.lr[0]);
+        }
+    }
+    for (int i = 0; i < v->num_instances; ++i)
+    {
+        int code = ~0, rootRef = -1;
+        if (instRoot[i] >= 0)
+        {
+            lf_status st = wide_level(c, B, instRoot[i], true, &code);
+            if (st != LF_OK) return st;
+            rootRef = instRoot[i];
+        }
+        float cf, rf;
+        std::memcpy(&cf, &code, 4);
+        std::memcpy(&rf, &rootRef, 4);
+        inst[(size_t)i * 4 + 3].z = cf;
+        inst[(size_t)i * 4 + 3].w = rf;
+    }
+    lf_status st = wide_level(c, B, v->top_level_index, false, wroot);
+    if (st != LF_OK) return st;
+    wrecs.swap(B.recs);
+    parent.assign(v->num_nodes, -1);
+    for (int i = 0; i < v->num_nodes; ++i)
+        if ((int)nodes[i].lr[2] == 0)
+        {
+            const int l = (int)nodes[i].lr[0], r = (int)nodes[i].lr[1];
+            if (l >= 0 && l < v->num_nodes) parent[l] = i;
+            if (r >= 0 && r < v->num_nodes) parent[r] = i;
+        }
+    return LF_OK;
+}
+
 void make_light(const float* l15, DevLight& d)
 {
     using lfc::v3;
@@ -343,6 +525,14 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     int tlasRoot = 0;
     lf_status st = encode_instances(c, v, nodes, recs, map, inst, sinst, &tlasRoot);
     if (st != LF_OK) return st;
+    std::vector<float4> wrecs;
+    std::vector<int> parent;
+    int wroot = 0;
+    st = encode_wide(c, v, nodes, inst, wrecs, parent, &wroot);
+    if (st != LF_OK) return st;
+    // room for a re-encoded instance level after instance updates (at most one wide node per
+    // inner node of the instance tree)
+    const size_t wideCap = wrecs.size() / kWideF4 + (size_t)v->num_instances;
 
     // triangles in packed order: v0, v1 - v0, v2 - v0
     std::vector<float4> tris((size_t)v->num_tris * 3);
@@ -391,6 +581,12 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     A(&d_norms, (size_t)v->num_vertices);
     A(&d_mats, (size_t)v->num_materials);
     A(&d_sinst, sinst.size());
+    float4* d_wide = nullptr;
+    float* d_refNodes = nullptr;
+    int* d_parent = nullptr;
+    A(&d_wide, wideCap * kWideF4);
+    A(&d_refNodes, (size_t)v->num_nodes * 9);
+    A(&d_parent, (size_t)v->num_nodes);
     float* d_env = nullptr;
     float2 *d_marg = nullptr, *d_cond = nullptr;
     uint8_t* d_tex = nullptr;
@@ -420,6 +616,9 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     H2D(d_norms, v->normals_uvy, (size_t)v->num_vertices * 16);
     H2D(d_mats, v->materials, (size_t)v->num_materials * sizeof(DevMaterial));
     H2D(d_sinst, sinst.data(), sinst.size() * sizeof(ShadeInstance));
+    H2D(d_wide, wrecs.data(), wrecs.size() * sizeof(float4));
+    H2D(d_refNodes, v->nodes, (size_t)v->num_nodes * 9 * sizeof(float));
+    H2D(d_parent, parent.data(), parent.size() * sizeof(int));
     if (hasEnv)
     {
         H2D(d_env, v->env_rgb, (size_t)v->env_width * v->env_height * 3 * sizeof(float));
@@ -445,6 +644,11 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     S.trav.numInstances = v->num_instances;
     S.trav.cullRel = 1.0e-4f;
     S.trav.cullAbs = 64.0f * ulp_of(extent);
+    S.trav.wnodes = d_wide;
+    S.trav.wroot = wroot;
+    S.trav.wideOn = 1;
+    S.trav.refNodes = d_refNodes;
+    S.trav.refParent = d_parent;
     S.vertIndices = d_vidx;
     S.vertices = d_verts;
     S.normals = d_norms;
@@ -477,6 +681,10 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     }
     sc->d_nodes = d_nodes;
     sc->nodeCapacity = recs.size() / 4;
+    sc->d_wide = d_wide;
+    sc->wideCapacity = wideCap;
+    sc->d_refNodes = d_refNodes;
+    sc->d_parent = d_parent;
     sc->d_instances = d_inst;
     sc->d_sinst = d_sinst;
     sc->d_materials = d_mats;
@@ -506,7 +714,17 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     lf_status st = encode_instances(c, v, nodes, recs, map, inst, sinst, &tlasRoot);
     if (st != LF_OK) return st;
     if (recs.size() / 4 > sc->nodeCapacity) return fail(c, LF_ERR_INVALID, "instance update grew the node array");
+    std::vector<float4> wrecs;
+    std::vector<int> parent;
+    int wroot = 0;
+    st = encode_wide(c, v, nodes, inst, wrecs, parent, &wroot);
+    if (st != LF_OK) return st;
+    if (wrecs.size() / kWideF4 > sc->wideCapacity) return fail(c, LF_ERR_INVALID, "instance update grew the wide tree");
     cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(sc->d_wide, wrecs.data(), wrecs.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(sc->d_refNodes, v->nodes, (size_t)v->num_nodes * 9 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(sc->d_parent, parent.data(), parent.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_nodes, recs.data(), recs.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_instances, inst.data(), inst.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_sinst, sinst.data(), sinst.size() * sizeof(ShadeInstance), cudaMemcpyHostToDevice);
@@ -515,6 +733,7 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     if (e != cudaSuccess) return cuda_fail(c, e, "instance update");
     sc->view.trav.root = tlasRoot;
     sc->view.trav.numNodes = (int)(recs.size() / 4);
+    sc->view.trav.wroot = wroot;
     return LF_OK;
 }
 
@@ -528,6 +747,16 @@ lf_status lf_scene_release(lf_scene* sc)
     }
     for (void* p : sc->allocs) cudaFree(p);
     delete sc;
+    return LF_OK;
+}
+
+lf_status lf_scene_set_traversal(lf_scene* sc, int32_t wide)
+{
+    if (!sc || (wide != 0 && wide != 1)) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(sc->ctx->mu);
+    cudaSetDevice(sc->ctx->device);
+    cudaStreamSynchronize(sc->ctx->stream);
+    sc->view.trav.wideOn = wide;
     return LF_OK;
 }
 

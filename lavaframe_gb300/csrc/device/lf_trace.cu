@@ -147,6 +147,44 @@ __global__ void __launch_bounds__(128) trace_persistent_kernel(DevScene S, const
     }
 }
 
+// Wide-tree form: each lane traces its ray to completion; warps take rays 32 at a time from a
+// global counter (in `perm` order), so a warp that finished early takes more work.
+template <bool kAny>
+__global__ void __launch_bounds__(128) trace_fetch_wide_kernel(DevScene S, const float4* rays, const int* perm,
+                                                               long long n, int4* hits, uint8_t* occluded, int lights,
+                                                               unsigned long long* next, uint32_t* status)
+{
+    const int lane = threadIdx.x & 31;
+    while (true)
+    {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(next, 32ull);
+        base = __shfl_sync(kFullMask, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const unsigned long long my = base + lane;
+        if (my < (unsigned long long)n)
+        {
+            const long long rid = perm ? (long long)perm[my] : (long long)my;
+            const float4 o4 = rays[2 * rid], d4 = rays[2 * rid + 1];
+            const v3 o(o4.x, o4.y, o4.z), d(d4.x, d4.y, d4.z);
+            Hit h;
+            uint32_t err;
+            if (kAny)
+            {
+                bool occ;
+                err = any_hit<false>(S, o, d, d4.w, lights != 0, &occ, &h, nullptr);
+                occluded[rid] = occ ? 1 : 0;
+            }
+            else
+            {
+                err = closest_hit<false>(S, o, d, d4.w, lights != 0, &h, nullptr);
+                hits[rid] = make_int4(__float_as_int(h.t), h.inst, h.prim, h.light);
+            }
+            if (err) atomicOr(status, err);
+        }
+    }
+}
+
 int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void* out, bool any, int lights,
                         const float lo[3], const float hi[3], bool binning, uint32_t* keys, uint32_t* hist, int* perm,
                         unsigned long long* next, uint32_t* status, cudaStream_t st)
@@ -169,6 +207,22 @@ int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void
     }
     cudaMemsetAsync(next, 0, sizeof(unsigned long long), st);
     int per_sm = 0;
+    if (S.wnodes && S.wideOn)
+    {
+        if (any)
+        {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fetch_wide_kernel<true>, 128, 0);
+            trace_fetch_wide_kernel<true><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
+                S, rays, order, n, nullptr, (uint8_t*)out, lights, next, status);
+        }
+        else
+        {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fetch_wide_kernel<false>, 128, 0);
+            trace_fetch_wide_kernel<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
+                S, rays, order, n, (int4*)out, nullptr, lights, next, status);
+        }
+        return (int)cudaGetLastError();
+    }
     if (any)
     {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_persistent_kernel<true>, 128, 0);

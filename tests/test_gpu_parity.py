@@ -30,10 +30,12 @@ def compare_hits(dev, ref):
     return int((~same).sum())
 
 
+@pytest.mark.parametrize("wide", [True, False])
 @pytest.mark.parametrize("culling", [True, False])
-def test_closest_hit_ids_bit_exact_on_soup(ctx, culling):
+def test_closest_hit_ids_bit_exact_on_soup(ctx, culling, wide):
     s = lf.HostScene().gen_soup(1 << 14, 10, 1).build()
     ds = ctx.upload(s)
+    ds.set_traversal(wide)
     if not culling:
         ds.set_culling(-1.0, 0.0)
     rays = soup_rays(s, 1 << 18)
@@ -262,3 +264,56 @@ def test_gpu_paths_equal_reference_shader(ctx, name):
     f.close()
     ds.close()
     assert same.all(), f"{(~same).sum()} of {same.size} paths differ"
+
+
+def tie_scene():
+    """A 16 x 16 grid of squares in the plane z = 0.5, two triangles each, instanced twice with
+    the same identity transform (a third instance is shifted): every hit has an exact twin in the
+    other instance, and rays through grid lines hit two adjacent triangles at the same distance."""
+    s = lf.HostScene()
+    n = 16
+    verts, norms = [], []
+    for i in range(n):
+        for j in range(n):
+            x0, x1, y0, y1 = i / n, (i + 1) / n, j / n, (j + 1) / n
+            for (a, b, c) in (((x0, y0), (x1, y0), (x1, y1)), ((x0, y0), (x1, y1), (x0, y1))):
+                for p in (a, b, c):
+                    verts.append([p[0], p[1], 0.5, 0.0])
+                    norms.append([0.0, 0.0, 1.0, 0.0])
+    mid = s.add_mesh(np.array(verts), np.array(norms))
+    m28 = np.zeros(28, np.float32)
+    m28[0:3] = 0.8
+    m28[6] = 1.0          # roughness
+    mat = s.add_material(m28)
+    eye = np.eye(4, dtype=np.float32)
+    s.add_instance(mid, eye.ravel(), mat)
+    s.add_instance(mid, eye.ravel(), mat)
+    shifted = eye.copy()
+    shifted[3, 2] = 0.25
+    s.add_instance(mid, shifted.ravel(), mat)
+    s.set_camera([0.5, 0.5, 2.0], [0.5, 0.5, 0.0], 45.0)
+    return s.build()
+
+
+def test_equal_distance_hits_follow_the_reference_order(ctx):
+    s = tie_scene()
+    ds = ctx.upload(s)
+    g = np.arange(0, 17) / 16.0
+    pts = np.array([(x, y) for x in g for y in g] + [((i + 0.5) / 16, j / 16) for i in range(16) for j in range(17)] +
+                   [((i + 0.3) / 16, (i + 0.3) / 16) for i in range(16)], np.float32)
+    rays = []
+    for (x, y) in pts:
+        for dz, oz in ((-1.0, 2.0), (1.0, -1.0)):
+            rays.append([x, y, oz, 0, 0, 0, dz, 1e6])
+        d = np.array([0.3, -0.2, -1.0], np.float32)
+        d /= np.float32(np.sqrt(np.float32((d * d).sum())))
+        o = np.array([x, y, 0.5], np.float32) - d * np.float32(1.5)
+        rays.append([o[0], o[1], o[2], 0, d[0], d[1], d[2], 1e6])
+    rays = np.array(rays, np.float32)
+    ref, _ = oracle.trace_closest(s.view(), rays)
+    hit = ref["prim"] >= 0
+    assert hit.mean() > 0.5
+    for flags in (0, lf.TRACE_SIMPLE):
+        dev = ctx.trace_closest(ds, rays, flags=flags)
+        assert compare_hits(dev, ref) == 0
+    ds.close()
