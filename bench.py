@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768; 0 = 768)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
+    ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
     ap.add_argument("--c4-ref-spp", type=int, default=4096, help="guiding workload reference samples")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
@@ -241,7 +242,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False):
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True):
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -252,6 +253,7 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False):
         spp = spp or 16
     p = s.render_params()
     ds = ctx.upload(s)
+    ds.set_traversal(wide)
     tuned = None
     if tune:
         from lavaframe_gb300 import autotune
@@ -462,7 +464,7 @@ def main():
         return
     if args.workload != "microbench":
         r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags,
-                         tune=args.autotune)
+                         tune=args.autotune, wide=args.traversal == "wide")
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)
@@ -472,6 +474,7 @@ def main():
     nrays = 1 << args.rays_log2
     rays, root = soup_rays(s, nrays)
     ds = ctx.upload(s)
+    ds.set_traversal(args.traversal == "wide")
     L = lf.lib()
     import ctypes as C
 

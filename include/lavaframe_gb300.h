@@ -276,6 +276,30 @@ lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend
 /* Current pool size and device bytes of the engine (0, 0 before first use). */
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 
+/* ------------------------------------------------------------------ post-process and export
+ * The display pass (postprocess.glsl:26-171 with TiledRenderer's uniforms): accumulated sum /
+ * samples (optionally with chromatic aberration), tone map 0..6 (none, linear, ACES,
+ * Reinhard, Kanjero, Hejl-Richard, Uncharted 2) with the shader's gamma, optional vignette,
+ * then the 8-bit conversion GetOutputBuffer reads (clamp to [0, 1], round to nearest). Fields
+ * follow RenderOptions (Renderer.h:18-67); `preview` is the camera-moving flag (no CA). */
+typedef struct lf_post_params
+{
+    int32_t tonemap;
+    int32_t use_ca, use_ca_distortion, use_vignette, preview;
+    float ca_distance, ca_p1, ca_p2, ca_p3;
+    float vignette_intensity, vignette_power;
+} lf_post_params;
+
+/* rgb8 (W*H*3 bytes) and/or rgbf (W*H*3 floats, after tone map and vignette, before the
+ * 8-bit conversion); row 0 = bottom as in GL. `samples` = the accumulated sample count. */
+lf_status lf_frame_postprocess(lf_frame* f, const lf_post_params* p, int32_t samples, uint8_t* rgb8, float* rgbf);
+/* Image export (Export.h:14-151 writes through stb/tinyexr; here): PNG (8-bit RGB), PPM (8-bit
+ * RGB) and PFM (float RGB). Input rows are bottom-first as the frame buffers; PNG and PPM are
+ * written top row first (the reference flips on write), PFM bottom-first as the format wants. */
+lf_status lf_write_png(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
+lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
+lf_status lf_write_pfm(const char* path, const float* rgbf, int32_t width, int32_t height);
+
 /* Render without allocating (no counterpart in the reference). For callers that cannot
  * allocate device memory while rendering - plugin hosts that hand out a fixed arena,
  * frame loops that forbid allocation, work recorded into CUDA graphs. Accumulates samples

@@ -191,20 +191,27 @@ public:
         for (size_t i = 0; i < (size_t)w_ * h_ * 3; ++i) (*data)[i] = (*data)[i] * inv;
     }
 
-    // 8-bit output with the default ACES fit and 1/2.2 gamma of postprocess.glsl:34-43,138-140.
+    // 8-bit output of the display pass (postprocess.glsl:26-171) with the scene's RenderOptions:
+    // tone map, chromatic aberration and vignette, row 0 at the bottom (caller delete[]s).
     void GetOutputBuffer(unsigned char** data, int& w, int& h) override
     {
-        float* hdr = nullptr;
-        GetOutputBufferHDR(&hdr, w, h);
-        *data = new unsigned char[(size_t)w * h * 3];
-        for (size_t i = 0; i < (size_t)w * h * 3; ++i)
-        {
-            float c = hdr[i];
-            float m = (c * (2.51f * c + 0.03f)) / (c * (2.43f * c + 0.59f) + 0.14f);
-            m = m < 0.f ? 0.f : (m > 1.f ? 1.f : m);
-            (*data)[i] = (unsigned char)(std::pow(m, 1.0f / 2.2f) * 255.0f);
-        }
-        delete[] hdr;
+        w = w_;
+        h = h_;
+        const auto& o = scene_->renderOptions;
+        lf_post_params pp;
+        pp.tonemap = o.tonemapIndex;
+        pp.use_ca = o.useCA ? 1 : 0;
+        pp.use_ca_distortion = o.useCADistortion ? 1 : 0;
+        pp.use_vignette = o.useVignette ? 1 : 0;
+        pp.preview = 0;
+        pp.ca_distance = o.caDistance;
+        pp.ca_p1 = o.caP1;
+        pp.ca_p2 = o.caP2;
+        pp.ca_p3 = o.caP3;
+        pp.vignette_intensity = o.vignetteIntensity;
+        pp.vignette_power = o.vignettePower;
+        *data = new unsigned char[(size_t)w_ * h_ * 3];
+        check(lf_frame_postprocess(frame_, &pp, sampleCounter_, *data, nullptr), "lf_frame_postprocess");
     }
 
     uint32_t SetViewport(int, int) override { return 0; }

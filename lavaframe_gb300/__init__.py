@@ -95,6 +95,10 @@ _SIG = {
     "lf_frame_set_batch": (C.c_int, [_P, C.c_int32]),
     "lf_frame_release": (C.c_int, [_P]),
     "lf_render_noalloc": (C.c_int, [_P, _P, C.c_int32, C.c_int32, _P]),
+    "lf_frame_postprocess": (C.c_int, [_P, _P, C.c_int32, _P, _F]),
+    "lf_write_png": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
+    "lf_write_ppm": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
+    "lf_write_pfm": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32]),
     "lf_server_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
     "lf_server_remove_scene": (C.c_int, [_P, C.c_int64]),
@@ -417,6 +421,32 @@ class DeviceScene:
             self.h = _P()
 
 
+class PostParams(C.Structure):
+    """lf_post_params: RenderOptions' display settings (tonemap 0..6, CA, vignette)."""
+    _fields_ = [("tonemap", C.c_int32), ("use_ca", C.c_int32), ("use_ca_distortion", C.c_int32),
+                ("use_vignette", C.c_int32), ("preview", C.c_int32), ("ca_distance", C.c_float),
+                ("ca_p1", C.c_float), ("ca_p2", C.c_float), ("ca_p3", C.c_float),
+                ("vignette_intensity", C.c_float), ("vignette_power", C.c_float)]
+
+    @classmethod
+    def defaults(cls, tonemap=2):
+        """RenderOptions' defaults (Renderer.h:25-44)."""
+        return cls(tonemap, 0, 0, 0, 0, 0.05, 5.0, -0.5, 0.5, 0.0, 1.0)
+
+
+def write_image(path, img):
+    """PNG / PPM from (H, W, 3) uint8, PFM from float32; row 0 = bottom."""
+    path = str(path)
+    h, w = img.shape[:2]
+    if path.endswith(".pfm"):
+        a = np.ascontiguousarray(img, np.float32)
+        _chk(lib().lf_write_pfm(path.encode(), _fp(a), w, h))
+    else:
+        a = np.ascontiguousarray(img, np.uint8)
+        fn = lib().lf_write_ppm if path.endswith(".ppm") else lib().lf_write_png
+        _chk(fn(path.encode(), a.ctypes.data_as(_P), w, h))
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget", C.c_uint64), ("paths_per_pass", C.c_int32), ("passes_per_job", C.c_int32)]
 
@@ -593,6 +623,14 @@ class Frame:
 
     def set_batch(self, spp):
         self.ctx._c(lib().lf_frame_set_batch(self.h, spp))
+
+    def postprocess(self, samples, params=None):
+        """Display pass: (rgb8, rgbf) of the accumulated sum over `samples`, row 0 = bottom."""
+        params = params or PostParams.defaults()
+        rgb8 = np.empty((self.params.height, self.params.width, 3), np.uint8)
+        rgbf = np.empty((self.params.height, self.params.width, 3), np.float32)
+        self.ctx._c(lib().lf_frame_postprocess(self.h, C.byref(params), samples, rgb8.ctypes.data_as(_P), _fp(rgbf)))
+        return rgb8, rgbf
 
     def set_guide(self, guide, alpha=0.5, train_every=4, lr=1e-2):
         """Guided rendering with `guide` (None detaches); trains on every train_every-th sample."""

@@ -29,6 +29,7 @@ def lib():
                                  C.c_float, P]
         L.lfo_math.argtypes = [C.c_int32, P, P, C.c_int64, P]
         L.lfo_rand_sequence.argtypes = [C.c_float, C.c_float, C.c_int32, C.c_uint32, C.c_int32, P]
+        L.lfo_postprocess.argtypes = [P, C.c_int32, C.c_int32, P, C.c_int32, P, P]
         _lib = L
     return _lib
 
@@ -87,3 +88,14 @@ def render(view, params, first_sample, num_samples, accum=None, want_paths=False
                      paths.ctypes.data if paths is not None else None, row_stride, row_offset, threads, cull_rel,
                      cull_abs, ctr.ctypes.data)
     return accum, paths, ctr
+
+
+def postprocess(accum_rgb, params, samples):
+    """postprocess.glsl on a (H, W, 3) accumulated sum: returns (rgb8, rgbf), row 0 = bottom.
+    `params` is a lavaframe_gb300.PostParams (same field layout as the oracle's)."""
+    acc = np.ascontiguousarray(accum_rgb, np.float32)
+    h, w = acc.shape[:2]
+    rgb8 = np.empty((h, w, 3), np.uint8)
+    rgbf = np.empty((h, w, 3), np.float32)
+    lib().lfo_postprocess(acc.ctypes.data, w, h, C.addressof(params), samples, rgb8.ctypes.data, rgbf.ctypes.data)
+    return rgb8, rgbf

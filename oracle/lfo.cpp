@@ -1351,3 +1351,146 @@ int lfo_rand_sequence(float px, float py, int32_t frame, uint32_t seed_fold, int
     return 0;
 }
 }
+
+// ------------------------------------------------------------------ post-process
+// postprocess.glsl:26-171 per output pixel, with TiledRenderer's uniforms
+// (TiledRenderer.cpp:540-552): GLSL vec4 arithmetic written per component, texture() as the
+// accumulation texture's GL_LINEAR / GL_REPEAT sampling (texel centres at +0.5), and the 8-bit
+// framebuffer conversion round(clamp(c) * 255) that GetOutputBuffer reads.
+namespace
+{
+struct PostIn
+{
+    int32_t tonemap, use_ca, use_ca_distortion, use_vignette, preview;
+    float ca_distance, ca_p1, ca_p2, ca_p3, vignette_intensity, vignette_power;
+};
+
+int wrap(int i, int n)
+{
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+// vec4 texture(pathTraceTexture, uv) of a W x H RGB (alpha 0) image
+void texture4(const float* rgb, int W, int H, float u, float v, float out[4])
+{
+    float xf = u * (float)W - 0.5f, yf = v * (float)H - 0.5f;
+    float fx = std::floor(xf), fy = std::floor(yf);
+    float a = xf - fx, b = yf - fy;
+    int x0 = wrap((int)fx, W), x1 = wrap((int)fx + 1, W), y0 = wrap((int)fy, H), y1 = wrap((int)fy + 1, H);
+    for (int k = 0; k < 3; ++k)
+    {
+        float t00 = rgb[((size_t)y0 * W + x0) * 3 + k], t10 = rgb[((size_t)y0 * W + x1) * 3 + k];
+        float t01 = rgb[((size_t)y1 * W + x0) * 3 + k], t11 = rgb[((size_t)y1 * W + x1) * 3 + k];
+        out[k] = (t00 * (1.0f - a) + t10 * a) * (1.0f - b) + (t01 * (1.0f - a) + t11 * a) * b;
+    }
+    out[3] = 0.0f;
+}
+
+float glsl_distance(float ax, float ay, float bx, float by)
+{
+    float dx = ax - bx, dy = ay - by;
+    return std::sqrt(dx * dx + dy * dy);
+}
+}
+
+extern "C" int lfo_postprocess(const float* accum_rgb, int32_t W, int32_t H, const void* params, int32_t samples,
+                               uint8_t* rgb8, float* rgbf)
+{
+    const PostIn& P = *reinterpret_cast<const PostIn*>(params);
+    const float invSampleCounter = 1.0f / (float)samples;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+        {
+            const float tu = ((float)x + 0.5f) / (float)W, tv = ((float)y + 0.5f) / (float)H;   // TexCoords
+            float color[4], t[4];
+            if (!P.preview && P.use_ca)
+            {
+                // chromaticAberration()
+                float offset = P.ca_distance;
+                float dist = 0.0f + lfc::pow_c(glsl_distance(tu, tv, P.ca_p3, P.ca_p3), P.ca_p1) * P.ca_p2;
+                float s;
+                if (P.use_ca_distortion)
+                    s = offset * dist;
+                else
+                {
+                    offset = offset * 0.025f;
+                    s = offset * P.ca_p2;
+                }
+                texture4(accum_rgb, W, H, tu + s, tv + s, t);
+                color[0] = t[0] * invSampleCounter;
+                texture4(accum_rgb, W, H, tu, tv, t);
+                color[1] = t[1] * invSampleCounter;
+                texture4(accum_rgb, W, H, tu - s, tv - s, t);
+                color[2] = t[2] * invSampleCounter;
+                color[3] = 0.0f;
+            }
+            else
+            {
+                texture4(accum_rgb, W, H, tu, tv, t);
+                for (int k = 0; k < 4; ++k) color[k] = t[k] * invSampleCounter;
+            }
+            const float gamma = 1.0f / 2.2f;
+            switch (P.tonemap)
+            {
+            case 1:
+            {
+                float luminance = 0.3f * color[0] + 0.6f * color[1] + 0.1f * color[2];
+                for (int k = 0; k < 4; ++k) color[k] = lfc::pow_c(color[k] * 1.0f / (1.0f + luminance / 2.0f), gamma);
+                break;
+            }
+            case 2:
+                for (int k = 0; k < 4; ++k)
+                {
+                    float c = color[k];
+                    color[k] = lfc::pow_c(lfc::clamp_g((c * (2.51f * c + 0.03f)) / (c * (2.43f * c + 0.59f) + 0.14f), 0.0f, 1.0f),
+                                          gamma);
+                }
+                break;
+            case 3:
+                for (int k = 0; k < 4; ++k) color[k] = lfc::pow_c(lfc::clamp_g(color[k] / (color[k] + 1.0f), 0.0f, 1.0f), gamma);
+                break;
+            case 4:
+                for (int k = 0; k < 4; ++k)
+                {
+                    float c = color[k];
+                    c = lfc::pow_c((c * (c * (1.2295f * c + 0.3135f) + 1.1935f * 0.4655f) / (c * (1.1935f * c + 0.4655f) + 0.073f)),
+                                   1.7f);
+                    if (k < 3) c = lfc::pow_c(c, 1.0f / 0.8f);
+                    c = c * 0.8f;
+                    color[k] = lfc::pow_c(lfc::clamp_g(c, 0.0f, 1.0f), gamma);
+                }
+                break;
+            case 5:
+                for (int k = 0; k < 4; ++k)
+                {
+                    float c = lfc::fmax_g(0.0f, color[k] - 0.004f);
+                    color[k] = (c * (6.2f * c + 0.5f)) / (c * (6.2f * c + 1.7f) + 0.06f);
+                }
+                break;
+            case 6:
+                for (int k = 0; k < 4; ++k)
+                {
+                    float c = color[k];
+                    float u2 = ((c * (0.15f * c + 0.10f * 0.50f) + 0.20f * 0.02f) / (c * (0.15f * c + 0.50f) + 0.20f * 0.30f)) -
+                               0.02f / 0.30f;
+                    color[k] = lfc::pow_c(u2, gamma) * 1.75f;
+                }
+                break;
+            default:
+                break;
+            }
+            if (P.use_vignette)
+            {
+                float d = 1.0f - lfc::pow_c(glsl_distance(tu, tv, 0.5f, 0.5f), P.vignette_power) * P.vignette_intensity;
+                for (int k = 0; k < 4; ++k) color[k] = color[k] * d;
+            }
+            const size_t i = (size_t)y * W + x;
+            for (int k = 0; k < 3; ++k)
+            {
+                if (rgbf) rgbf[i * 3 + k] = color[k];
+                if (rgb8) rgb8[i * 3 + k] = (uint8_t)std::nearbyint(lfc::clamp_g(color[k], 0.0f, 1.0f) * 255.0f);
+            }
+        }
+    return 0;
+}

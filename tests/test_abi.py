@@ -44,14 +44,16 @@ def test_struct_layouts_match_header(tmp_path):
         pytest.skip("no C compiler")
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lavaframe_gb300.h"\n'
-                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lf_scene_view),'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lf_scene_view),'
                    ' sizeof(lf_render_params), sizeof(lf_hit), offsetof(lf_render_params, seed),'
                    ' offsetof(lf_scene_view, env_width), sizeof(lf_server_config), sizeof(lf_job_info),'
-                   ' sizeof(lf_server_stats), offsetof(lf_server_stats, scenes_resident));return 0;}')
+                   ' sizeof(lf_server_stats), offsetof(lf_server_stats, scenes_resident), sizeof(lf_post_params));'
+                   'return 0;}')
     exe = tmp_path / "sz"
     subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [C.sizeof(lf.SceneView), C.sizeof(lf.RenderParams), lf.HIT_DTYPE.itemsize,
             lf.RenderParams.seed.offset, lf.SceneView.env_width.offset, C.sizeof(lf.ServerConfig),
-            C.sizeof(lf.JobInfo), C.sizeof(lf.ServerStats), lf.ServerStats.scenes_resident.offset]
+            C.sizeof(lf.JobInfo), C.sizeof(lf.ServerStats), lf.ServerStats.scenes_resident.offset,
+            C.sizeof(lf.PostParams)]
     assert got == want

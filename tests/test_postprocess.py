@@ -1,0 +1,143 @@
+"""Post-process and export (postprocess.glsl, Export.h): the oracle against a float32 numpy
+restatement of the shader's formulas (CPU), the GPU pass against the oracle bit for bit, and
+the PNG / PFM writers by reading the files back."""
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+import lavaframe_gb300 as lf
+import oracle
+from tests import scenes
+
+F = np.float32
+
+
+def np_texture(img, u, v):
+    """GL_LINEAR + GL_REPEAT sampling of an (H, W, 3) image at (u, v) arrays."""
+    h, w = img.shape[:2]
+    xf = u * F(w) - F(0.5)
+    yf = v * F(h) - F(0.5)
+    fx, fy = np.floor(xf), np.floor(yf)
+    a, b = (xf - fx)[..., None], (yf - fy)[..., None]
+    x0, y0 = fx.astype(np.int64) % w, fy.astype(np.int64) % h
+    x1, y1 = (x0 + 1) % w, (y0 + 1) % h
+    top = img[y0, x0] * (F(1) - a) + img[y0, x1] * a
+    bot = img[y1, x0] * (F(1) - a) + img[y1, x1] * a
+    return top * (F(1) - b) + bot * b
+
+
+def np_post(acc, p, samples):
+    h, w = acc.shape[:2]
+    u = ((np.arange(w, dtype=F) + F(0.5)) / F(w))[None, :].repeat(h, 0)
+    v = ((np.arange(h, dtype=F) + F(0.5)) / F(h))[:, None].repeat(w, 1)
+    inv = F(1.0) / F(samples)
+    if p.use_ca and not p.preview:
+        dist = np.sqrt((u - F(p.ca_p3)) ** 2 + (v - F(p.ca_p3)) ** 2).astype(F) ** F(p.ca_p1) * F(p.ca_p2)
+        s = F(p.ca_distance) * dist if p.use_ca_distortion else np.full_like(u, F(p.ca_distance) * F(0.025) * F(p.ca_p2))
+        c = np.stack([np_texture(acc, u + s, v + s)[..., 0], np_texture(acc, u, v)[..., 1],
+                      np_texture(acc, u - s, v - s)[..., 2]], -1) * inv
+    else:
+        c = np_texture(acc, u, v) * inv
+    g = F(1.0) / F(2.2)
+    t = p.tonemap
+    if t == 1:
+        lum = F(0.3) * c[..., 0] + F(0.6) * c[..., 1] + F(0.1) * c[..., 2]
+        c = (c / (F(1) + lum / F(2))[..., None]) ** g
+    elif t == 2:
+        c = np.clip((c * (F(2.51) * c + F(0.03))) / (c * (F(2.43) * c + F(0.59)) + F(0.14)), 0, 1) ** g
+    elif t == 3:
+        c = np.clip(c / (c + F(1)), 0, 1) ** g
+    elif t == 4:
+        c = ((c * (c * (F(1.2295) * c + F(0.3135)) + F(1.1935) * F(0.4655))) /
+             (c * (F(1.1935) * c + F(0.4655)) + F(0.073))) ** F(1.7)
+        c = np.clip(c ** (F(1) / F(0.8)) * F(0.8), 0, 1) ** g
+    elif t == 5:
+        c = np.maximum(F(0), c - F(0.004))
+        c = (c * (F(6.2) * c + F(0.5))) / (c * (F(6.2) * c + F(1.7)) + F(0.06))
+    elif t == 6:
+        c = ((c * (F(0.15) * c + F(0.05)) + F(0.004)) / (c * (F(0.15) * c + F(0.5)) + F(0.06)) - F(0.02) / F(0.3))
+        c = c ** g * F(1.75)
+    if p.use_vignette:
+        d = F(1) - np.sqrt((u - F(0.5)) ** 2 + (v - F(0.5)) ** 2) ** F(p.vignette_power) * F(p.vignette_intensity)
+        c = c * d[..., None]
+    return c.astype(F)
+
+
+def settings():
+    out = []
+    for t in range(7):
+        out.append(lf.PostParams.defaults(t))
+    p = lf.PostParams.defaults(2)
+    p.use_vignette, p.vignette_intensity, p.vignette_power = 1, 0.7, 1.5
+    out.append(p)
+    p = lf.PostParams.defaults(3)
+    p.use_ca, p.ca_distance = 1, 0.5
+    out.append(p)
+    p = lf.PostParams.defaults(1)
+    p.use_ca, p.use_ca_distortion, p.ca_distance = 1, 1, 0.8
+    out.append(p)
+    return out
+
+
+def test_oracle_postprocess_matches_the_shader_formulas():
+    rng = np.random.default_rng(0)
+    acc = (rng.gamma(1.5, 1.0, (24, 40, 3)) * 16).astype(np.float32)
+    for p in settings():
+        _, got = oracle.postprocess(acc, p, 16)
+        ref = np_post(acc, p, 16)
+        np.testing.assert_allclose(got, ref, rtol=2e-5, atol=2e-6, err_msg=str(p.tonemap))
+
+
+def read_png(path):
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, w, h = 8, b"", 0, 0
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        assert zlib.crc32(typ + body) == struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0]
+        if typ == b"IHDR":
+            w, h = struct.unpack(">II", body[:8])
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    raw = zlib.decompress(idat)
+    rows = [raw[y * (3 * w + 1) + 1:(y + 1) * (3 * w + 1)] for y in range(h)]
+    return np.frombuffer(b"".join(rows), np.uint8).reshape(h, w, 3)
+
+
+def test_png_and_pfm_writers_round_trip(tmp_path):
+    rng = np.random.default_rng(1)
+    img8 = rng.integers(0, 256, (70, 300, 3), dtype=np.uint8)   # > 64 KiB: several stored blocks
+    lf.write_image(tmp_path / "a.png", img8)
+    back = read_png(tmp_path / "a.png")
+    assert np.array_equal(back, img8[::-1])                      # written top row first
+    imgf = rng.normal(size=(5, 7, 3)).astype(np.float32)
+    lf.write_image(tmp_path / "a.pfm", imgf)
+    raw = open(tmp_path / "a.pfm", "rb").read()
+    hdr = b"PF\n7 5\n-1.0\n"
+    assert raw.startswith(hdr)
+    assert np.array_equal(np.frombuffer(raw[len(hdr):], "<f4").reshape(5, 7, 3), imgf)
+
+
+@pytest.mark.gpu
+def test_gpu_postprocess_is_bit_exact(ctx):
+    s = scenes.build("cornell")
+    p = s.render_params()
+    p.width, p.height = 80, 56
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p)
+    f.render(0, 8)
+    f.sync()
+    acc = f.accum()
+    try:
+        for pp in settings():
+            rgb8, rgbf = f.postprocess(8, pp)
+            o8, of = oracle.postprocess(acc, pp, 8)
+            assert rgbf.view(np.uint32).tobytes() == of.view(np.uint32).tobytes(), pp.tonemap
+            assert np.array_equal(rgb8, o8)
+    finally:
+        f.close()
+        ds.close()
