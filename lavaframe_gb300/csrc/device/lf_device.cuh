@@ -51,13 +51,18 @@ struct DevLight
     float pad[3];
 };
 
-// 4-wide nodes collapsed from the reference's binary tree (see traverse_wide): per node
+// Wide nodes collapsed from the reference's binary tree (see traverse_wide): per node
 // 2 * kWide float4 = [min x | max x | min y | max y | min z | max z | child codes | child
-// reference-node indices], kWide values per group; unused slots have code kWideEmpty.
-constexpr int kWide = 4;
+// reference-node indices], kWide values per group (kWide / 4 float4 each); unused slots have
+// code kWideEmpty. The width is a build option (LF_WIDE = 4 or 8).
+#ifndef LF_WIDE
+#define LF_WIDE 4
+#endif
+constexpr int kWide = LF_WIDE;
+static_assert(kWide == 4 || kWide == 8, "wide nodes have 4 or 8 children");
 constexpr int kWideF4 = 2 * kWide;
 constexpr int kWideEmpty = (int)0x80000002;
-constexpr int kWideStack = 96;
+constexpr int kWideStack = kWide == 8 ? 160 : 96;
 
 struct DevScene
 {
@@ -612,23 +617,37 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             continue;
         }
         const float4* rec = S.wnodes + (size_t)code * kWideF4;
-        const float4 mnx = ldg4(rec + 0), mxx = ldg4(rec + 1), mny = ldg4(rec + 2), mxy = ldg4(rec + 3);
-        const float4 mnz = ldg4(rec + 4), mxz = ldg4(rec + 5), cc = ldg4(rec + 6), rr = ldg4(rec + 7);
+        constexpr int G = kWide / 4;   // float4 per group
+        float g[8][kWide];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int h4 = 0; h4 < G; ++h4)
+            {
+                const float4 f = ldg4(rec + q * G + h4);
+                g[q][h4 * 4 + 0] = f.x;
+                g[q][h4 * 4 + 1] = f.y;
+                g[q][h4 * 4 + 2] = f.z;
+                g[q][h4 * 4 + 3] = f.w;
+            }
         const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
-        const float bx0[4] = {mnx.x, mnx.y, mnx.z, mnx.w}, bx1[4] = {mxx.x, mxx.y, mxx.z, mxx.w};
-        const float by0[4] = {mny.x, mny.y, mny.z, mny.w}, by1[4] = {mxy.x, mxy.y, mxy.z, mxy.w};
-        const float bz0[4] = {mnz.x, mnz.y, mnz.z, mnz.w}, bz1[4] = {mxz.x, mxz.y, mxz.z, mxz.w};
-        const int cds[4] = {__float_as_int(cc.x), __float_as_int(cc.y), __float_as_int(cc.z), __float_as_int(cc.w)};
-        const int rfs[4] = {__float_as_int(rr.x), __float_as_int(rr.y), __float_as_int(rr.z), __float_as_int(rr.w)};
-        float hd[4];
-        int hc[4], hr[4];
+        float hd[kWide];
+        int hc[kWide], hr[kWide];
         int nh = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < kWide; ++j)
         {
+            const float* bx0 = g[0];
+            const float* bx1 = g[1];
+            const float* by0 = g[2];
+            const float* by1 = g[3];
+            const float* bz0 = g[4];
+            const float* bz1 = g[5];
+            const int cdj = __float_as_int(g[6][j]);
+            const int rfj = __float_as_int(g[7][j]);
             float e;
             const float h = box_hit_fast(bx0[j], by0[j], bz0[j], bx1[j], by1[j], bz1[j], ro, invd, &e);
-            if (cds[j] != kWideEmpty && h > 0.f && e <= lim)
+            if (cdj != kWideEmpty && h > 0.f && e <= lim)
             {
                 // insertion by entry distance, nearest first
                 int k = nh++;
@@ -640,8 +659,8 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                     --k;
                 }
                 hd[k] = e;
-                hc[k] = cds[j];
-                hr[k] = rfs[j];
+                hc[k] = cdj;
+                hr[k] = rfj;
             }
         }
         if (nh == 0)

@@ -351,7 +351,9 @@ lf_status wide_level(lf_ctx* c, WideBuilder& B, int start, bool meshLevel, int* 
             std::memcpy(&f[7][j], &refIdx, 4);
         }
         float4* o = &B.recs[(size_t)rec * kWideF4];
-        for (int g = 0; g < 8; ++g) o[g] = make_float4(f[g][0], f[g][1], f[g][2], f[g][3]);
+        for (int g = 0; g < 8; ++g)
+            for (int h4 = 0; h4 < kWide / 4; ++h4)
+                o[g * (kWide / 4) + h4] = make_float4(f[g][h4 * 4], f[g][h4 * 4 + 1], f[g][h4 * 4 + 2], f[g][h4 * 4 + 3]);
     }
     *rootCode = B.map[start];
     return LF_OK;
