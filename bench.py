@@ -536,11 +536,14 @@ def main():
         peak, peak_kind = measured_peaks()
         launch_s = ms / 1e3 / args.steps
         achieved = bpr * nrays / launch_s / 1e9
-        prof = ROOT / "profiles" / "c2_trace_closest_traffic.json"
+        # DRAM bytes per ray from the committed ncu summary of the traversal kernel (a reduced case
+        # captured under the size rule), scaled to this launch by its ray count
+        prof = ROOT / "profiles" / "c2_trace_wide_small.md"
         traffic = None
         if prof.exists():
-            pj = json.loads(prof.read_text())
-            traffic = pj.get("dram_bytes_per_ray", 0) * nrays
+            for line in prof.read_text().splitlines():
+                if line.startswith("dram_bytes_per_ray:"):
+                    traffic = float(line.split(":")[1].split()[0]) * nrays
         if not args.no_extras:
             for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8)):
                 try:
