@@ -81,6 +81,8 @@ struct DevScene
     int wideOn;
     const float* refNodes;      // the reference's 36-byte nodes, for tie resolution
     const int* refParent;       // parent of every reference node, -1 at roots
+    const int* leafOfTri;       // reference leaf node of every packed triangle
+    const int* leafOfInst;      // reference instance-level leaf node of every instance
 };
 
 struct TraceStats
@@ -414,7 +416,7 @@ static __device__ __noinline__ bool ref_first(const DevScene& S, int a, int b, v
 // (world ray wo / winvd, reference nodes of the two instances' leaves).
 template <bool kAny>
 __device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, int inst, v3 ro, v3 rd, float* tio,
-                                             Hit* out, bool* anyHit, v3 wo, v3 winvd, int instRef, int bestInstRef)
+                                             Hit* out, bool* anyHit, v3 wo, v3 winvd)
 {
     int stack[kStackSize];
     int sp = 0;
@@ -442,7 +444,7 @@ __device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, in
                 float u, v;
                 const float tt = tri_hit(S.tris + (size_t)(first + i) * 3, ro, rd, &u, &v);
                 const bool tie = !kAny && tt == t && tt >= 0.f && out->prim >= 0 && out->inst != inst &&
-                                 ref_first(S, instRef, bestInstRef, wo, winvd);
+                                 ref_first(S, S.leafOfInst[inst], S.leafOfInst[out->inst], wo, winvd);
                 if ((tt >= 0.f && tt < t) || tie)
                 {
                     t = tt;
@@ -499,12 +501,11 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
     if (!fast) return traverse<kAny, false>(S, o, d, tBest, out, nullptr);
     const int kBlasEnd = (int)0x80000000;
     const int kEmpty = (int)0x80000001;
-    int2 stack[kWideStack];   // (code, reference node)
+    int stack[kWideStack];
     int sp = 0;
-    int code = S.wroot, cref = -1;
+    int code = S.wroot;
     bool meshLevel = false;
-    int curInst = -1, curInstRef = -1;
-    int bestLeafRef = -1, bestInstRef = -1;
+    int curInst = -1;
     v3 ro = o, rd = d, invd = winvd;
     uint32_t err = 0;
     const bool cull = S.cullRel >= 0.f;
@@ -516,9 +517,7 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
         if (code == kEmpty)
         {
             if (sp == 0) break;
-            const int2 e = stack[--sp];
-            code = e.x;
-            cref = e.y;
+            code = stack[--sp];
             if (code == kBlasEnd)
             {
                 meshLevel = false;
@@ -547,9 +546,12 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                         {
                             // equal distance: the reference keeps the one it reaches first
                             if (curInst == out->inst)
-                                take = cref == bestLeafRef ? prim < out->prim : ref_first(S, cref, bestLeafRef, ro, invd);
+                            {
+                                const int la = S.leafOfTri[prim], lb = S.leafOfTri[out->prim];
+                                take = la == lb ? prim < out->prim : ref_first(S, la, lb, ro, invd);
+                            }
                             else
-                                take = ref_first(S, curInstRef, bestInstRef, o, winvd);
+                                take = ref_first(S, S.leafOfInst[curInst], S.leafOfInst[out->inst], o, winvd);
                         }
                         if (take)
                         {
@@ -557,8 +559,6 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                             out->prim = prim;
                             out->inst = curInst;
                             out->light = -1;
-                            bestLeafRef = cref;
-                            bestInstRef = curInstRef;
                             if (kAny)
                             {
                                 *tBest = t;
@@ -582,19 +582,12 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                 const v3 iinvd = inv_dir(ird, &ofast);
                 if (!ofast)
                 {
-                    const int before = out->prim;
-                    const int beforeInst = out->inst;
                     bool anyHit = false;
-                    err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd, cref, bestInstRef);
+                    err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd);
                     if (kAny && anyHit)
                     {
                         *tBest = t;
                         return err;
-                    }
-                    if (out->prim != before || out->inst != beforeInst)
-                    {
-                        bestLeafRef = -1;   // no later hit of this instance can tie with it
-                        bestInstRef = cref;
                     }
                     code = kEmpty;
                     continue;
@@ -604,23 +597,21 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                     err |= LF_DEVERR_STACK;
                     break;
                 }
-                stack[sp++] = make_int2(kBlasEnd, -1);
+                stack[sp++] = kBlasEnd;
                 ro = iro;
                 rd = ird;
                 invd = iinvd;
                 meshLevel = true;
                 curInst = inst;
-                curInstRef = cref;
                 code = __float_as_int(e3.z);
-                cref = __float_as_int(e3.w);
             }
             continue;
         }
         const float4* rec = S.wnodes + (size_t)code * kWideF4;
         constexpr int G = kWide / 4;   // float4 per group
-        float g[8][kWide];
+        float g[7][kWide];   // the eighth group (reference indices) is not needed here
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
+        for (int q = 0; q < 7; ++q)
 #pragma unroll
             for (int h4 = 0; h4 < G; ++h4)
             {
@@ -632,7 +623,7 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             }
         const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
         float hd[kWide];
-        int hc[kWide], hr[kWide];
+        int hc[kWide];
         int nh = 0;
 #pragma unroll
         for (int j = 0; j < kWide; ++j)
@@ -644,7 +635,6 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             const float* bz0 = g[4];
             const float* bz1 = g[5];
             const int cdj = __float_as_int(g[6][j]);
-            const int rfj = __float_as_int(g[7][j]);
             float e;
             const float h = box_hit_fast(bx0[j], by0[j], bz0[j], bx1[j], by1[j], bz1[j], ro, invd, &e);
             if (cdj != kWideEmpty && h > 0.f && e <= lim)
@@ -655,12 +645,10 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                 {
                     hd[k] = hd[k - 1];
                     hc[k] = hc[k - 1];
-                    hr[k] = hr[k - 1];
                     --k;
                 }
                 hd[k] = e;
                 hc[k] = cdj;
-                hr[k] = rfj;
             }
         }
         if (nh == 0)
@@ -673,9 +661,8 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             err |= LF_DEVERR_STACK;
             break;
         }
-        for (int k = nh - 1; k >= 1; --k) stack[sp++] = make_int2(hc[k], hr[k]);
+        for (int k = nh - 1; k >= 1; --k) stack[sp++] = hc[k];
         code = hc[0];
-        cref = hr[0];
     }
     *tBest = t;
     return err;

@@ -69,6 +69,8 @@ struct lf_scene
     size_t wideCapacity = 0;        // wide records allocated
     float* d_refNodes = nullptr;    // the reference nodes (tie resolution)
     int* d_parent = nullptr;
+    int* d_leafOfTri = nullptr;     // reference leaf of every triangle
+    int* d_leafOfInst = nullptr;    // reference leaf of every instance
     float boundsLo[3] = {0, 0, 0}, boundsHi[3] = {0, 0, 0};   // instance-level root box
 };
 

@@ -360,9 +360,11 @@ lf_status wide_level(lf_ctx* c, WideBuilder& B, int start, bool meshLevel, int* 
 }
 
 // Wide tree of the whole scene (mesh levels first, then the instance level), the instance
-// records' wide root codes and mesh root reference nodes, and the reference parent array.
+// records' wide root codes and mesh root reference nodes, the reference parent array and the
+// reference leaf that holds each triangle and each instance (tie resolution only).
 lf_status encode_wide(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, std::vector<float4>& inst,
-                      std::vector<float4>& wrecs, std::vector<int>& parent, int* wroot)
+                      std::vector<float4>& wrecs, std::vector<int>& parent, std::vector<int>& leafOfTri,
+                      std::vector<int>& leafOfInst, int* wroot)
 {
     WideBuilder B;
     B.nodes = nodes;
@@ -405,13 +407,24 @@ lf_status encode_wide(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, s
     if (st != LF_OK) return st;
     wrecs.swap(B.recs);
     parent.assign(v->num_nodes, -1);
+    leafOfTri.assign(std::max(v->num_tris, 1), -1);
+    leafOfInst.assign(std::max(v->num_instances, 1), -1);
     for (int i = 0; i < v->num_nodes; ++i)
-        if ((int)nodes[i].lr[2] == 0)
+    {
+        const int z = (int)nodes[i].lr[2];
+        const int l = (int)nodes[i].lr[0], r = (int)nodes[i].lr[1];
+        if (z == 0)
         {
-            const int l = (int)nodes[i].lr[0], r = (int)nodes[i].lr[1];
             if (l >= 0 && l < v->num_nodes) parent[l] = i;
             if (r >= 0 && r < v->num_nodes) parent[r] = i;
         }
+        else if (z > 0)
+        {
+            for (int t = std::max(l, 0); t < l + r && t < v->num_tris; ++t) leafOfTri[t] = i;
+        }
+        else if (-z - 1 < v->num_instances)
+            leafOfInst[-z - 1] = i;
+    }
     return LF_OK;
 }
 
@@ -528,9 +541,9 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     lf_status st = encode_instances(c, v, nodes, recs, map, inst, sinst, &tlasRoot);
     if (st != LF_OK) return st;
     std::vector<float4> wrecs;
-    std::vector<int> parent;
+    std::vector<int> parent, leafOfTri, leafOfInst;
     int wroot = 0;
-    st = encode_wide(c, v, nodes, inst, wrecs, parent, &wroot);
+    st = encode_wide(c, v, nodes, inst, wrecs, parent, leafOfTri, leafOfInst, &wroot);
     if (st != LF_OK) return st;
     // room for a re-encoded instance level after instance updates (at most one wide node per
     // inner node of the instance tree)
@@ -586,9 +599,12 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     float4* d_wide = nullptr;
     float* d_refNodes = nullptr;
     int* d_parent = nullptr;
+    int *d_leafOfTri = nullptr, *d_leafOfInst = nullptr;
     A(&d_wide, wideCap * kWideF4);
     A(&d_refNodes, (size_t)v->num_nodes * 9);
     A(&d_parent, (size_t)v->num_nodes);
+    A(&d_leafOfTri, leafOfTri.size());
+    A(&d_leafOfInst, leafOfInst.size());
     float* d_env = nullptr;
     float2 *d_marg = nullptr, *d_cond = nullptr;
     uint8_t* d_tex = nullptr;
@@ -621,6 +637,8 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     H2D(d_wide, wrecs.data(), wrecs.size() * sizeof(float4));
     H2D(d_refNodes, v->nodes, (size_t)v->num_nodes * 9 * sizeof(float));
     H2D(d_parent, parent.data(), parent.size() * sizeof(int));
+    H2D(d_leafOfTri, leafOfTri.data(), leafOfTri.size() * sizeof(int));
+    H2D(d_leafOfInst, leafOfInst.data(), leafOfInst.size() * sizeof(int));
     if (hasEnv)
     {
         H2D(d_env, v->env_rgb, (size_t)v->env_width * v->env_height * 3 * sizeof(float));
@@ -651,6 +669,8 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     S.trav.wideOn = 1;
     S.trav.refNodes = d_refNodes;
     S.trav.refParent = d_parent;
+    S.trav.leafOfTri = d_leafOfTri;
+    S.trav.leafOfInst = d_leafOfInst;
     S.vertIndices = d_vidx;
     S.vertices = d_verts;
     S.normals = d_norms;
@@ -687,6 +707,8 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     sc->wideCapacity = wideCap;
     sc->d_refNodes = d_refNodes;
     sc->d_parent = d_parent;
+    sc->d_leafOfTri = d_leafOfTri;
+    sc->d_leafOfInst = d_leafOfInst;
     sc->d_instances = d_inst;
     sc->d_sinst = d_sinst;
     sc->d_materials = d_mats;
@@ -717,9 +739,9 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     if (st != LF_OK) return st;
     if (recs.size() / 4 > sc->nodeCapacity) return fail(c, LF_ERR_INVALID, "instance update grew the node array");
     std::vector<float4> wrecs;
-    std::vector<int> parent;
+    std::vector<int> parent, leafOfTri, leafOfInst;
     int wroot = 0;
-    st = encode_wide(c, v, nodes, inst, wrecs, parent, &wroot);
+    st = encode_wide(c, v, nodes, inst, wrecs, parent, leafOfTri, leafOfInst, &wroot);
     if (st != LF_OK) return st;
     if (wrecs.size() / kWideF4 > sc->wideCapacity) return fail(c, LF_ERR_INVALID, "instance update grew the wide tree");
     cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -727,6 +749,10 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     if (e == cudaSuccess)
         e = cudaMemcpy(sc->d_refNodes, v->nodes, (size_t)v->num_nodes * 9 * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_parent, parent.data(), parent.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(sc->d_leafOfTri, leafOfTri.data(), leafOfTri.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(sc->d_leafOfInst, leafOfInst.data(), leafOfInst.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_nodes, recs.data(), recs.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_instances, inst.data(), inst.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(sc->d_sinst, sinst.data(), sinst.size() * sizeof(ShadeInstance), cudaMemcpyHostToDevice);
