@@ -493,6 +493,52 @@ __device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, in
     return err;
 }
 
+// Child hits of one wide node, nearest entry first: hc[0..nh).
+__device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 invd, float lim, int* hc)
+{
+    const float4* rec = S.wnodes + (size_t)code * kWideF4;
+    constexpr int G = kWide / 4;   // float4 per group
+    float g[7][kWide];   // the eighth group (reference indices) is not needed here
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+#pragma unroll
+        for (int h4 = 0; h4 < G; ++h4)
+        {
+            const float4 f = ldg4(rec + q * G + h4);
+            g[q][h4 * 4 + 0] = f.x;
+            g[q][h4 * 4 + 1] = f.y;
+            g[q][h4 * 4 + 2] = f.z;
+            g[q][h4 * 4 + 3] = f.w;
+        }
+    float hd[kWide];
+    int nh = 0;
+#pragma unroll
+    for (int j = 0; j < kWide; ++j)
+    {
+        const int cdj = __float_as_int(g[6][j]);
+        float e;
+        const float h = box_hit_fast(g[0][j], g[2][j], g[4][j], g[1][j], g[3][j], g[5][j], ro, invd, &e);
+        if (cdj != kWideEmpty && h > 0.f && e <= lim)
+        {
+            // insertion by entry distance, nearest first
+            int k = nh++;
+            while (k > 0 && hd[k - 1] > e)
+            {
+                hd[k] = hd[k - 1];
+                hc[k] = hc[k - 1];
+                --k;
+            }
+            hd[k] = e;
+            hc[k] = cdj;
+        }
+    }
+    return nh;
+}
+
+// Two-level traversal of the wide tree, one node or leaf per step with the stack pop folded
+// into the same step. Leaves are triangle runs on the mesh level and instances on the instance
+// level; entering an instance pushes a marker and switches to the object-space ray. Equal-
+// distance hits are ordered by the reference's own visiting order (ref_first).
 template <bool kAny>
 __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d, float* tBest, Hit* out)
 {
@@ -503,7 +549,7 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
     const int kEmpty = (int)0x80000001;
     int stack[kWideStack];
     int sp = 0;
-    int code = S.wroot;
+    int code = S.wroot;   // >= 0 inner record, < 0 leaf, kEmpty none
     bool meshLevel = false;
     int curInst = -1;
     v3 ro = o, rd = d, invd = winvd;
@@ -514,89 +560,79 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
     while (true)
     {
         if (++steps > kMaxTraversalSteps) { err |= LF_DEVERR_STEPS; break; }
-        if (code == kEmpty)
+        if (code >= 0)
         {
-            if (sp == 0) break;
-            code = stack[--sp];
-            if (code == kBlasEnd)
-            {
-                meshLevel = false;
-                ro = o;
-                rd = d;
-                invd = winvd;
-                code = kEmpty;
-            }
-            continue;
+            int hc[kWide];
+            const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
+            const int nh = wide_node(S, code, ro, invd, lim, hc);
+            if (sp + nh - 1 > kWideStack) { err |= LF_DEVERR_STACK; break; }
+            for (int k = nh - 1; k >= 1; --k) stack[sp++] = hc[k];
+            code = nh > 0 ? hc[0] : kEmpty;
         }
-        if (code < 0)
+        else if (meshLevel)
         {
             const int payload = ~code;
-            if (meshLevel)
+            const int first = payload >> 2, cnt = payload & 3;
+            code = kEmpty;
+            for (int i = 0; i < cnt; ++i)
             {
-                const int first = payload >> 2, cnt = payload & 3;
-                for (int i = 0; i < cnt; ++i)
+                float u, v;
+                const int prim = first + i;
+                const float tt = tri_hit(S.tris + (size_t)prim * 3, ro, rd, &u, &v);
+                if (tt >= 0.f && tt <= t)
                 {
-                    float u, v;
-                    const int prim = first + i;
-                    const float tt = tri_hit(S.tris + (size_t)prim * 3, ro, rd, &u, &v);
-                    if (tt >= 0.f && tt <= t)
+                    bool take = tt < t;
+                    if (!take && !kAny && out->prim >= 0)
                     {
-                        bool take = tt < t;
-                        if (!take && !kAny && out->prim >= 0)
+                        // equal distance: the reference keeps the one it reaches first
+                        if (curInst == out->inst)
                         {
-                            // equal distance: the reference keeps the one it reaches first
-                            if (curInst == out->inst)
-                            {
-                                const int la = S.leafOfTri[prim], lb = S.leafOfTri[out->prim];
-                                take = la == lb ? prim < out->prim : ref_first(S, la, lb, ro, invd);
-                            }
-                            else
-                                take = ref_first(S, S.leafOfInst[curInst], S.leafOfInst[out->inst], o, winvd);
+                            const int la = S.leafOfTri[prim], lb = S.leafOfTri[out->prim];
+                            take = la == lb ? prim < out->prim : ref_first(S, la, lb, ro, invd);
                         }
-                        if (take)
+                        else
+                            take = ref_first(S, S.leafOfInst[curInst], S.leafOfInst[out->inst], o, winvd);
+                    }
+                    if (take)
+                    {
+                        t = tt;
+                        out->prim = prim;
+                        out->inst = curInst;
+                        out->light = -1;
+                        if (kAny)
                         {
-                            t = tt;
-                            out->prim = prim;
-                            out->inst = curInst;
-                            out->light = -1;
-                            if (kAny)
-                            {
-                                *tBest = t;
-                                return err;
-                            }
+                            *tBest = t;
+                            return err;
                         }
                     }
                 }
-                code = kEmpty;
+            }
+        }
+        else
+        {
+            const int inst = ~code;
+            const float4* ir = S.instances + (size_t)inst * 4;
+            float m[12];
+            int root, mat;
+            load_instance(ir, m, &root, &mat);
+            const float4 e3 = ldg4(ir + 3);
+            const v3 iro = xform(m, o, 1.0f), ird = xform(m, d, 0.0f);
+            bool ofast;
+            const v3 iinvd = inv_dir(ird, &ofast);
+            code = kEmpty;
+            if (!ofast)
+            {
+                bool anyHit = false;
+                err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd);
+                if (kAny && anyHit)
+                {
+                    *tBest = t;
+                    return err;
+                }
             }
             else
             {
-                const int inst = payload;
-                const float4* ir = S.instances + (size_t)inst * 4;
-                float m[12];
-                int root, mat;
-                load_instance(ir, m, &root, &mat);
-                const float4 e3 = ldg4(ir + 3);
-                const v3 iro = xform(m, o, 1.0f), ird = xform(m, d, 0.0f);
-                bool ofast;
-                const v3 iinvd = inv_dir(ird, &ofast);
-                if (!ofast)
-                {
-                    bool anyHit = false;
-                    err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd);
-                    if (kAny && anyHit)
-                    {
-                        *tBest = t;
-                        return err;
-                    }
-                    code = kEmpty;
-                    continue;
-                }
-                if (sp >= kWideStack)
-                {
-                    err |= LF_DEVERR_STACK;
-                    break;
-                }
+                if (sp >= kWideStack) { err |= LF_DEVERR_STACK; break; }
                 stack[sp++] = kBlasEnd;
                 ro = iro;
                 rd = ird;
@@ -605,64 +641,22 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
                 curInst = inst;
                 code = __float_as_int(e3.z);
             }
-            continue;
         }
-        const float4* rec = S.wnodes + (size_t)code * kWideF4;
-        constexpr int G = kWide / 4;   // float4 per group
-        float g[7][kWide];   // the eighth group (reference indices) is not needed here
-#pragma unroll
-        for (int q = 0; q < 7; ++q)
-#pragma unroll
-            for (int h4 = 0; h4 < G; ++h4)
-            {
-                const float4 f = ldg4(rec + q * G + h4);
-                g[q][h4 * 4 + 0] = f.x;
-                g[q][h4 * 4 + 1] = f.y;
-                g[q][h4 * 4 + 2] = f.z;
-                g[q][h4 * 4 + 3] = f.w;
-            }
-        const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
-        float hd[kWide];
-        int hc[kWide];
-        int nh = 0;
-#pragma unroll
-        for (int j = 0; j < kWide; ++j)
+        if (code == kEmpty)
         {
-            const float* bx0 = g[0];
-            const float* bx1 = g[1];
-            const float* by0 = g[2];
-            const float* by1 = g[3];
-            const float* bz0 = g[4];
-            const float* bz1 = g[5];
-            const int cdj = __float_as_int(g[6][j]);
-            float e;
-            const float h = box_hit_fast(bx0[j], by0[j], bz0[j], bx1[j], by1[j], bz1[j], ro, invd, &e);
-            if (cdj != kWideEmpty && h > 0.f && e <= lim)
+            if (sp == 0) break;
+            code = stack[--sp];
+            if (code == kBlasEnd)
             {
-                // insertion by entry distance, nearest first
-                int k = nh++;
-                while (k > 0 && hd[k - 1] > e)
-                {
-                    hd[k] = hd[k - 1];
-                    hc[k] = hc[k - 1];
-                    --k;
-                }
-                hd[k] = e;
-                hc[k] = cdj;
+                // leave the instance; the entry below the marker is an instance-level one
+                meshLevel = false;
+                ro = o;
+                rd = d;
+                invd = winvd;
+                if (sp == 0) break;
+                code = stack[--sp];
             }
         }
-        if (nh == 0)
-        {
-            code = kEmpty;
-            continue;
-        }
-        if (sp + nh - 1 > kWideStack)
-        {
-            err |= LF_DEVERR_STACK;
-            break;
-        }
-        for (int k = nh - 1; k >= 1; --k) stack[sp++] = hc[k];
-        code = hc[0];
     }
     *tBest = t;
     return err;
