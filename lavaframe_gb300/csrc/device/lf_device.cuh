@@ -493,11 +493,23 @@ __device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, in
     return err;
 }
 
-// Child hits of one wide node, nearest entry first: hc[0..nh).
+__device__ __forceinline__ void sort2(uint32_t& a, uint32_t& b)
+{
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Child hits of one wide node, nearest entry first: hc[0..nh). The children are ordered by a
+// sorting network on keys that hold the entry distance's bits (entries are >= 0, so their bit
+// patterns order like the values) with the child slot in the low bits; children whose entries
+// differ only in those bits are ordered by slot. The visiting order only decides how early the
+// closest hit is found, not which hit is returned.
 __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 invd, float lim, int* hc)
 {
     const float4* rec = S.wnodes + (size_t)code * kWideF4;
     constexpr int G = kWide / 4;   // float4 per group
+    constexpr uint32_t kSlotMask = kWide - 1;
     float g[7][kWide];   // the eighth group (reference indices) is not needed here
 #pragma unroll
     for (int q = 0; q < 7; ++q)
@@ -510,7 +522,7 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
             g[q][h4 * 4 + 2] = f.z;
             g[q][h4 * 4 + 3] = f.w;
         }
-    float hd[kWide];
+    uint32_t key[kWide];
     int nh = 0;
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
@@ -518,19 +530,38 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
         const int cdj = __float_as_int(g[6][j]);
         float e;
         const float h = box_hit_fast(g[0][j], g[2][j], g[4][j], g[1][j], g[3][j], g[5][j], ro, invd, &e);
-        if (cdj != kWideEmpty && h > 0.f && e <= lim)
-        {
-            // insertion by entry distance, nearest first
-            int k = nh++;
-            while (k > 0 && hd[k - 1] > e)
-            {
-                hd[k] = hd[k - 1];
-                hc[k] = hc[k - 1];
-                --k;
-            }
-            hd[k] = e;
-            hc[k] = cdj;
-        }
+        const bool hit = cdj != kWideEmpty && h > 0.f && e <= lim;
+        key[j] = hit ? ((__float_as_uint(e) & ~kSlotMask) | (uint32_t)j) : 0xFFFFFFFFu;
+        nh += hit ? 1 : 0;
+    }
+    if constexpr (kWide == 4)
+    {
+        sort2(key[0], key[1]);
+        sort2(key[2], key[3]);
+        sort2(key[0], key[2]);
+        sort2(key[1], key[3]);
+        sort2(key[1], key[2]);
+    }
+    else
+    {
+        // Batcher's odd-even merge sort of 8
+#pragma unroll
+        for (int a = 0; a < 8; a += 2) sort2(key[a], key[a + 1]);
+        sort2(key[0], key[2]); sort2(key[1], key[3]); sort2(key[4], key[6]); sort2(key[5], key[7]);
+        sort2(key[1], key[2]); sort2(key[5], key[6]);
+        sort2(key[0], key[4]); sort2(key[1], key[5]); sort2(key[2], key[6]); sort2(key[3], key[7]);
+        sort2(key[2], key[4]); sort2(key[3], key[5]);
+        sort2(key[1], key[2]); sort2(key[3], key[4]); sort2(key[5], key[6]);
+    }
+#pragma unroll
+    for (int k = 0; k < kWide; ++k)
+    {
+        const uint32_t slot = key[k] & kSlotMask;
+        int c = __float_as_int(g[6][0]);
+#pragma unroll
+        for (int j = 1; j < kWide; ++j)
+            if (slot == (uint32_t)j) c = __float_as_int(g[6][j]);
+        hc[k] = c;
     }
     return nh;
 }
@@ -566,7 +597,9 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
             const int nh = wide_node(S, code, ro, invd, lim, hc);
             if (sp + nh - 1 > kWideStack) { err |= LF_DEVERR_STACK; break; }
-            for (int k = nh - 1; k >= 1; --k) stack[sp++] = hc[k];
+#pragma unroll
+            for (int k = kWide - 1; k >= 1; --k)
+                if (k < nh) stack[sp++] = hc[k];
             code = nh > 0 ? hc[0] : kEmpty;
         }
         else if (meshLevel)
