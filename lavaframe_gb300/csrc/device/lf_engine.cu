@@ -196,8 +196,10 @@ __global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
 }
 
 // ------------------------------------------------------------------ extend / shade / shadow
+// The traversal kernels are held to 72 registers (7 blocks of 128 threads per SM; a few spills)
+// whatever block size they are launched with.
 template <bool kOne>
-__global__ void engine_extend_kernel(EngineBuffers b, EngineJob one, int parity)
+__global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob one, int parity)
 {
     const int n = b.ctl->count[parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr[1], (unsigned long long)n);
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
 }
 
 template <bool kOne>
-__global__ void engine_shadow_kernel(EngineBuffers b, EngineJob one)
+__global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob one)
 {
     const int n = b.ctl->shadowCount;
     unsigned long long rays = 0;
