@@ -118,6 +118,8 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
     c->doneCount[parity] = 0;
     c->shadowCount = 0;
     c->count[parity ^ 1] = 0;
+    c->extendNext = 0;
+    c->shadowNext = 0;
 }
 
 // ------------------------------------------------------------------ finish / refill
@@ -204,8 +206,16 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
     const int n = b.ctl->count[parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr[1], (unsigned long long)n);
     const int* q = b.queue[parity];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    const int lane = threadIdx.x & 31;
+    while (true)
     {
+        // warps take queue entries 32 at a time, so long rays do not hold up a fixed share
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&b.ctl->extendNext, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        if (i >= n) continue;
         const int p = q[i];
         const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
         Hit h;
@@ -267,8 +277,15 @@ __global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob 
 {
     const int n = b.ctl->shadowCount;
     unsigned long long rays = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    const int lane = threadIdx.x & 31;
+    while (true)
     {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&b.ctl->shadowNext, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        if (i >= n) continue;
         const ShadowRec rec = b.shadow[i];
         if constexpr (kOne)
             set_error(b.status, shadow_path(one.S, one.P, b.ps, rec, rays));
