@@ -386,23 +386,26 @@ __device__ __forceinline__ uint32_t traverse(const DevScene& S, v3 o, v3 d, floa
 // True when the reference's depth-first traversal of the tree holding reference nodes a and b
 // reaches a before b: at their lowest common ancestor it descends into the child whose box
 // value is smaller (ties left, closest_hit.glsl:172-187), exact box test with the level's ray.
-static __device__ __noinline__ bool ref_first(const DevScene& S, int a, int b, v3 o, v3 invd)
+// Arguments are plain values (no reference to the scene) so that calling it leaves the caller's
+// registers alone.
+static __device__ __noinline__ bool ref_first_at(const int* parent, const float* refNodes, int a, int b, v3 o,
+                                                 v3 invd)
 {
     int da = 0, db = 0;
-    for (int x = a; S.refParent[x] >= 0 && da < 1024; x = S.refParent[x]) ++da;
-    for (int x = b; S.refParent[x] >= 0 && db < 1024; x = S.refParent[x]) ++db;
-    for (; da > db; --da) a = S.refParent[a];
-    for (; db > da; --db) b = S.refParent[b];
-    for (int g = 0; g < 1024 && a != b && S.refParent[a] != S.refParent[b]; ++g)
+    for (int x = a; parent[x] >= 0 && da < 1024; x = parent[x]) ++da;
+    for (int x = b; parent[x] >= 0 && db < 1024; x = parent[x]) ++db;
+    for (; da > db; --da) a = parent[a];
+    for (; db > da; --db) b = parent[b];
+    for (int g = 0; g < 1024 && a != b && parent[a] != parent[b]; ++g)
     {
-        a = S.refParent[a];
-        b = S.refParent[b];
+        a = parent[a];
+        b = parent[b];
     }
-    if (a == b || S.refParent[a] < 0) return false;
-    const float* P = S.refNodes + (size_t)S.refParent[a] * 9;
+    if (a == b || parent[a] < 0) return false;
+    const float* P = refNodes + (size_t)parent[a] * 9;
     const int l = (int)P[6], r = (int)P[7];
-    const float* Ln = S.refNodes + (size_t)l * 9;
-    const float* Rn = S.refNodes + (size_t)r * 9;
+    const float* Ln = refNodes + (size_t)l * 9;
+    const float* Rn = refNodes + (size_t)r * 9;
     float e;
     const float hL = box_hit(Ln[0], Ln[1], Ln[2], Ln[3], Ln[4], Ln[5], o, invd, &e);
     const float hR = box_hit(Rn[0], Rn[1], Rn[2], Rn[3], Rn[4], Rn[5], o, invd, &e);
@@ -410,12 +413,17 @@ static __device__ __noinline__ bool ref_first(const DevScene& S, int a, int b, v
     return a == nearC;
 }
 
+__device__ __forceinline__ bool ref_first(const DevScene& S, int a, int b, v3 o, v3 invd)
+{
+    return ref_first_at(S.refParent, S.refNodes, a, b, o, invd);
+}
+
 // Binary traversal of one mesh level (the reference's order and exact box test) for an
 // object-space ray whose direction is degenerate. Updates t / out like traverse; a hit at the
 // same distance as the best hit of another instance is resolved by the instance tree's order
 // (world ray wo / winvd, reference nodes of the two instances' leaves).
 template <bool kAny>
-__device__ __noinline__ uint32_t mesh_binary(const DevScene& S, int rootCode, int inst, v3 ro, v3 rd, float* tio,
+__device__ __noinline__ uint32_t mesh_binary(const DevScene S, int rootCode, int inst, v3 ro, v3 rd, float* tio,
                                              Hit* out, bool* anyHit, v3 wo, v3 winvd)
 {
     int stack[kStackSize];
@@ -655,8 +663,13 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             code = kEmpty;
             if (!ofast)
             {
+                // copies, so that t and the hit record keep no address and stay in registers
                 bool anyHit = false;
-                err |= mesh_binary<kAny>(S, root, inst, iro, ird, &t, out, &anyHit, o, winvd);
+                float tm = t;
+                Hit hm = *out;
+                err |= mesh_binary<kAny>(S, root, inst, iro, ird, &tm, &hm, &anyHit, o, winvd);
+                t = tm;
+                *out = hm;
                 if (kAny && anyHit)
                 {
                     *tBest = t;
