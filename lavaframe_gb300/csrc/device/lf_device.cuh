@@ -196,6 +196,27 @@ __device__ __forceinline__ float tri_hit(const float4* tri, v3 o, v3 d, float* p
     return ok ? uz : -1.0f;
 }
 
+// tri_hit for a hit that only counts at distances in [0, tmax]: the distance quotient is formed
+// first and the two barycentric quotients only when it is in range. Each quotient is the same
+// IEEE division as in tri_hit, so a hit is reported exactly when tri_hit reports it with
+// t <= tmax.
+__device__ __forceinline__ float tri_hit_upto(const float4* tri, v3 o, v3 d, float tmax)
+{
+    float4 a = ldg4(tri + 0), b = ldg4(tri + 1), c = ldg4(tri + 2);
+    v3 v0(a.x, a.y, a.z), e0(b.x, b.y, b.z), e1(c.x, c.y, c.z);
+    v3 p = lfc::cross(d, e1);
+    float det = lfc::dot(e0, p);
+    v3 tv = o - v0;
+    v3 q = lfc::cross(tv, e0);
+    float uz = lfc::dot(e1, q) / det;
+    if (!(uz >= 0.0f && uz <= tmax)) return -1.0f;
+    float ux = lfc::dot(tv, p) / det;
+    float uy = lfc::dot(d, q) / det;
+    float uw = 1.0f - ux - uy;
+    bool ok = ux >= 0.0f && uy >= 0.0f && uw >= 0.0f;
+    return ok ? uz : -1.0f;
+}
+
 // Instance inverse transform applied like `vec3(inverse(M) * vec4(x, w))`.
 __device__ __forceinline__ void load_instance(const float4* rec, float m[12], int* root, int* mat)
 {
@@ -617,10 +638,9 @@ __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d,
             code = kEmpty;
             for (int i = 0; i < cnt; ++i)
             {
-                float u, v;
                 const int prim = first + i;
-                const float tt = tri_hit(S.tris + (size_t)prim * 3, ro, rd, &u, &v);
-                if (tt >= 0.f && tt <= t)
+                const float tt = tri_hit_upto(S.tris + (size_t)prim * 3, ro, rd, t);
+                if (tt >= 0.f)
                 {
                     bool take = tt < t;
                     if (!take && !kAny && out->prim >= 0)
