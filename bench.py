@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
+    ap.add_argument("--render-size", default="", help="c1/c3 workloads: override the resolution WxH (profiling)")
     ap.add_argument("--c4-ref-spp", type=int, default=4096, help="guiding workload reference samples")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
@@ -242,7 +243,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True):
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True, size=None):
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -252,6 +253,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
         s = lf.HostScene().gen_icospheres(64 if which == "c3full" else 13, 6, 3, 1024, 512).build()
         spp = spp or 16
     p = s.render_params()
+    if size:
+        p.width, p.height = size
     ds = ctx.upload(s)
     ds.set_traversal(wide)
     tuned = None
@@ -463,8 +466,9 @@ def main():
         ctx.close()
         return
     if args.workload != "microbench":
+        size = tuple(int(x) for x in args.render_size.split("x")) if args.render_size else None
         r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags,
-                         tune=args.autotune, wide=args.traversal == "wide")
+                         tune=args.autotune, wide=args.traversal == "wide", size=size)
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)

@@ -119,6 +119,7 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
     c->shadowCount = 0;
     c->count[parity ^ 1] = 0;
     c->extendNext = 0;
+    c->shadeNext = 0;
     c->shadowNext = 0;
 }
 
@@ -241,15 +242,20 @@ template <bool kOne, int kThreadsPerSm>
 __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
     engine_shade_kernel(EngineBuffers b, EngineJob one, int parity)
 {
-    __shared__ int smem[33];
     EngineCtl* ctl = b.ctl;
     const int n = ctl->count[parity];
     const int* qin = b.queue[parity];
     int* qout = b.queue[parity ^ 1];
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)   // block-uniform
+    const int lane = threadIdx.x & 31;
+    while (true)
     {
-        const int i = base + threadIdx.x;
+        // warps take 32 queue entries at a time and append their outputs with one atomic per
+        // queue, so no warp waits for the others of its block
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&ctl->shadeNext, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
         bool pushExt = false, pushShadow = false, finished = false;
         int p = -1;
         ShadowRec rec;
@@ -266,9 +272,10 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
             }
             finished = !pushExt;
         }
-        block_push(pushExt, p, qout, &ctl->count[parity ^ 1], b.cap, b.status, smem);
-        block_push(pushShadow, rec, b.shadow, &ctl->shadowCount, b.cap, b.status, smem);
-        block_push(finished, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
+        __syncwarp();
+        warp_push(pushExt, p, qout, &ctl->count[parity ^ 1], b.cap, b.status);
+        warp_push(pushShadow, rec, b.shadow, &ctl->shadowCount, b.cap, b.status);
+        warp_push(finished, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status);
     }
 }
 

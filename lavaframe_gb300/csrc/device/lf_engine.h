@@ -55,7 +55,7 @@ struct EngineCtl
     int active;                    // paths started and not yet written out
     int freeCount;                 // slots on the free list
     int taken;                     // slots the current step's refill started
-    int extendNext, shadowNext;    // work counters of the extend and shadow kernels
+    int extendNext, shadeNext, shadowNext;   // work counters of the extend, shade and shadow kernels
 };
 
 struct EngineBuffers

@@ -26,10 +26,15 @@
 #include <stdint.h>
 #include <string.h>
 
+// The transcendental functions (LF_HD_CALL) stay out of line on the device: the shading kernel
+// calls them from many places and inlining every copy costs more in instruction fetch than the
+// calls do.
 #if defined(__CUDACC__)
 #define LF_HD __host__ __device__ __forceinline__
+#define LF_HD_CALL static __host__ __device__ __noinline__
 #else
 #define LF_HD inline
+#define LF_HD_CALL inline
 #endif
 
 namespace lfc
@@ -118,7 +123,7 @@ LF_HD float reduce_pio2(float x, int* q)
     return ((x - k * C1) - k * C2) - k * C3;
 }
 
-LF_HD void sincos_c(float x, float* s, float* c)
+LF_HD_CALL void sincos_c(float x, float* s, float* c)
 {
     int q;
     float r = reduce_pio2(x, &q);
@@ -132,21 +137,21 @@ LF_HD void sincos_c(float x, float* s, float* c)
     }
 }
 
-LF_HD float sin_c(float x)
+LF_HD_CALL float sin_c(float x)
 {
     float s, c;
     sincos_c(x, &s, &c);
     return s;
 }
 
-LF_HD float cos_c(float x)
+LF_HD_CALL float cos_c(float x)
 {
     float s, c;
     sincos_c(x, &s, &c);
     return c;
 }
 
-LF_HD float tan_c(float x)
+LF_HD_CALL float tan_c(float x)
 {
     float s, c;
     sincos_c(x, &s, &c);
@@ -175,7 +180,7 @@ LF_HD float atan_unit(float t)
     return base + (t + (t * z) * p);
 }
 
-LF_HD float atan2_c(float y, float x)
+LF_HD_CALL float atan2_c(float y, float x)
 {
     if (x != x || y != y) return x + y;
     float ax = fabsf(x), ay = fabsf(y);
@@ -198,10 +203,10 @@ LF_HD float atan2_c(float y, float x)
     return (as_uint(y) >> 31) ? -a : a;
 }
 
-LF_HD float acos_c(float x) { return atan2_c(sqrtf((1.0f - x) * (1.0f + x)), x); }
+LF_HD_CALL float acos_c(float x) { return atan2_c(sqrtf((1.0f - x) * (1.0f + x)), x); }
 
 // ------------------------------------------------------------------ exp / log / pow
-LF_HD float exp_c(float x)
+LF_HD_CALL float exp_c(float x)
 {
     if (x != x) return x;
     if (x > 88.7228394f) return as_float(0x7f800000u);
@@ -221,7 +226,7 @@ LF_HD float exp_c(float x)
     return scale2(p, (int)k);
 }
 
-LF_HD float log_c(float x)
+LF_HD_CALL float log_c(float x)
 {
     if (x != x || x < 0.0f) return as_float(0x7fc00000u);
     if (x == 0.0f) return -as_float(0x7f800000u);
@@ -255,7 +260,7 @@ LF_HD float log_c(float x)
     return fe * L1 + (fe * L2 + lm);
 }
 
-LF_HD float pow_c(float x, float y)
+LF_HD_CALL float pow_c(float x, float y)
 {
     if (y == 0.0f || x == 1.0f) return 1.0f;
     if (x != x || y != y) return x + y;
