@@ -452,16 +452,16 @@ __device__ __forceinline__ uint32_t shadow_path(const ShadeScene& S, const Param
     Hit h;
     bool occ;
     uint32_t err = 0;
-    if (flags & 1u)
+    // the record's rays in order (environment first, then the light), through one traversal
+    // call site, so that lanes trace their first rays together
+    const int nr = __popc(flags & 3u);
+    for (int j = 0; j < nr; ++j)
     {
-        err |= any_hit<false>(S.trav, pos, f3(rec.c), kInfinity - kEps, lights, &occ, &h, nullptr);
-        if (!occ) Li = Li + f3(rec.e);
-        ++rays;
-    }
-    if (flags & 2u)
-    {
-        err |= any_hit<false>(S.trav, pos, f3(rec.f), rec.f.w, lights, &occ, &h, nullptr);
-        if (!occ) Li = Li + f3(rec.g);
+        const bool env = (flags & 1u) && j == 0;
+        const float4 dir = env ? rec.c : rec.f;
+        const float4 col = env ? rec.e : rec.g;
+        err |= any_hit<false>(S.trav, pos, f3(dir), env ? kInfinity - kEps : rec.f.w, lights, &occ, &h, nullptr);
+        if (!occ) Li = Li + f3(col);
         ++rays;
     }
     float4 L4 = ps.L[p];
