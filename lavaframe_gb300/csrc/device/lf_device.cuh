@@ -595,137 +595,175 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
     return nh;
 }
 
-// Two-level traversal of the wide tree, one node or leaf per step with the stack pop folded
-// into the same step. Leaves are triangle runs on the mesh level and instances on the instance
-// level; entering an instance pushes a marker and switches to the object-space ray. Equal-
-// distance hits are ordered by the reference's own visiting order (ref_first).
+// Two-level traversal of the wide tree as a state machine: wide_step visits one node or leaf
+// and folds the stack pop into the same step. Leaves are triangle runs on the mesh level and
+// instances on the instance level; entering an instance pushes a marker and switches to the
+// object-space ray. Equal-distance hits are ordered by the reference's own visiting order
+// (ref_first). The state lives in registers (the stack in local memory), so a persistent
+// kernel can interleave rays without saving it.
+struct WideRay
+{
+    v3 o, d, winvd;    // world-space ray
+    v3 ro, rd, invd;   // ray of the current level
+    float t;           // current end of the ray (best hit distance)
+    int code;          // next node: >= 0 inner record, < 0 leaf, kWideNone none
+    int sp, curInst, steps;
+    bool meshLevel;
+    uint32_t err;
+};
+
+constexpr int kWideBlasEnd = (int)0x80000000;   // stack marker: leave the instance
+constexpr int kWideNone = (int)0x80000001;
+
+// Starts a traversal of a ray with a regular inverse direction (inv_dir's `fast`).
+__device__ __forceinline__ void wide_init(const DevScene& S, WideRay& w, v3 o, v3 d, v3 winvd, float tmax)
+{
+    w.o = o;
+    w.d = d;
+    w.winvd = winvd;
+    w.ro = o;
+    w.rd = d;
+    w.invd = winvd;
+    w.t = tmax;
+    w.code = S.wroot;
+    w.sp = 0;
+    w.curInst = -1;
+    w.steps = 0;
+    w.meshLevel = false;
+    w.err = 0;
+}
+
+// One traversal step; returns true when the traversal has ended (w.t and `out` hold the result).
+template <bool kAny>
+__device__ __forceinline__ bool wide_step(const DevScene& S, WideRay& w, int* stack, Hit& out)
+{
+    if (++w.steps > kMaxTraversalSteps)
+    {
+        w.err |= LF_DEVERR_STEPS;
+        return true;
+    }
+    int code = w.code;
+    if (code >= 0)
+    {
+        int hc[kWide];
+        const float lim = S.cullRel >= 0.f ? w.t + w.t * S.cullRel + S.cullAbs : 3.4e38f;
+        const int nh = wide_node(S, code, w.ro, w.invd, lim, hc);
+        if (w.sp + nh - 1 > kWideStack)
+        {
+            w.err |= LF_DEVERR_STACK;
+            return true;
+        }
+#pragma unroll
+        for (int k = kWide - 1; k >= 1; --k)
+            if (k < nh) stack[w.sp++] = hc[k];
+        code = nh > 0 ? hc[0] : kWideNone;
+    }
+    else if (w.meshLevel)
+    {
+        const int payload = ~code;
+        const int first = payload >> 2, cnt = payload & 3;
+        code = kWideNone;
+        for (int i = 0; i < cnt; ++i)
+        {
+            const int prim = first + i;
+            const float tt = tri_hit_upto(S.tris + (size_t)prim * 3, w.ro, w.rd, w.t);
+            if (tt >= 0.f)
+            {
+                bool take = tt < w.t;
+                if (!take && !kAny && out.prim >= 0)
+                {
+                    // equal distance: the reference keeps the one it reaches first
+                    if (w.curInst == out.inst)
+                    {
+                        const int la = S.leafOfTri[prim], lb = S.leafOfTri[out.prim];
+                        take = la == lb ? prim < out.prim : ref_first(S, la, lb, w.ro, w.invd);
+                    }
+                    else
+                        take = ref_first(S, S.leafOfInst[w.curInst], S.leafOfInst[out.inst], w.o, w.winvd);
+                }
+                if (take)
+                {
+                    w.t = tt;
+                    out.prim = prim;
+                    out.inst = w.curInst;
+                    out.light = -1;
+                    if (kAny) return true;
+                }
+            }
+        }
+    }
+    else
+    {
+        const int inst = ~code;
+        const float4* ir = S.instances + (size_t)inst * 4;
+        float m[12];
+        int root, mat;
+        load_instance(ir, m, &root, &mat);
+        const float4 e3 = ldg4(ir + 3);
+        const v3 iro = xform(m, w.o, 1.0f), ird = xform(m, w.d, 0.0f);
+        bool ofast;
+        const v3 iinvd = inv_dir(ird, &ofast);
+        code = kWideNone;
+        if (!ofast)
+        {
+            // copies, so that the state keeps no address and stays in registers
+            bool anyHit = false;
+            float tm = w.t;
+            Hit hm = out;
+            w.err |= mesh_binary<kAny>(S, root, inst, iro, ird, &tm, &hm, &anyHit, w.o, w.winvd);
+            w.t = tm;
+            out = hm;
+            if (kAny && anyHit) return true;
+        }
+        else
+        {
+            if (w.sp >= kWideStack)
+            {
+                w.err |= LF_DEVERR_STACK;
+                return true;
+            }
+            stack[w.sp++] = kWideBlasEnd;
+            w.ro = iro;
+            w.rd = ird;
+            w.invd = iinvd;
+            w.meshLevel = true;
+            w.curInst = inst;
+            code = __float_as_int(e3.z);
+        }
+    }
+    if (code == kWideNone)
+    {
+        if (w.sp == 0) return true;
+        code = stack[--w.sp];
+        if (code == kWideBlasEnd)
+        {
+            // leave the instance; the entry below the marker is an instance-level one
+            w.meshLevel = false;
+            w.ro = w.o;
+            w.rd = w.d;
+            w.invd = w.winvd;
+            if (w.sp == 0) return true;
+            code = stack[--w.sp];
+        }
+    }
+    w.code = code;
+    return false;
+}
+
 template <bool kAny>
 __device__ __forceinline__ uint32_t traverse_wide(const DevScene& S, v3 o, v3 d, float* tBest, Hit* out)
 {
     bool fast;
     const v3 winvd = inv_dir(d, &fast);
     if (!fast) return traverse<kAny, false>(S, o, d, tBest, out, nullptr);
-    const int kBlasEnd = (int)0x80000000;
-    const int kEmpty = (int)0x80000001;
+    WideRay w;
     int stack[kWideStack];
-    int sp = 0;
-    int code = S.wroot;   // >= 0 inner record, < 0 leaf, kEmpty none
-    bool meshLevel = false;
-    int curInst = -1;
-    v3 ro = o, rd = d, invd = winvd;
-    uint32_t err = 0;
-    const bool cull = S.cullRel >= 0.f;
-    float t = *tBest;
-    int steps = 0;
-    while (true)
-    {
-        if (++steps > kMaxTraversalSteps) { err |= LF_DEVERR_STEPS; break; }
-        if (code >= 0)
-        {
-            int hc[kWide];
-            const float lim = cull ? t + t * S.cullRel + S.cullAbs : 3.4e38f;
-            const int nh = wide_node(S, code, ro, invd, lim, hc);
-            if (sp + nh - 1 > kWideStack) { err |= LF_DEVERR_STACK; break; }
-#pragma unroll
-            for (int k = kWide - 1; k >= 1; --k)
-                if (k < nh) stack[sp++] = hc[k];
-            code = nh > 0 ? hc[0] : kEmpty;
-        }
-        else if (meshLevel)
-        {
-            const int payload = ~code;
-            const int first = payload >> 2, cnt = payload & 3;
-            code = kEmpty;
-            for (int i = 0; i < cnt; ++i)
-            {
-                const int prim = first + i;
-                const float tt = tri_hit_upto(S.tris + (size_t)prim * 3, ro, rd, t);
-                if (tt >= 0.f)
-                {
-                    bool take = tt < t;
-                    if (!take && !kAny && out->prim >= 0)
-                    {
-                        // equal distance: the reference keeps the one it reaches first
-                        if (curInst == out->inst)
-                        {
-                            const int la = S.leafOfTri[prim], lb = S.leafOfTri[out->prim];
-                            take = la == lb ? prim < out->prim : ref_first(S, la, lb, ro, invd);
-                        }
-                        else
-                            take = ref_first(S, S.leafOfInst[curInst], S.leafOfInst[out->inst], o, winvd);
-                    }
-                    if (take)
-                    {
-                        t = tt;
-                        out->prim = prim;
-                        out->inst = curInst;
-                        out->light = -1;
-                        if (kAny)
-                        {
-                            *tBest = t;
-                            return err;
-                        }
-                    }
-                }
-            }
-        }
-        else
-        {
-            const int inst = ~code;
-            const float4* ir = S.instances + (size_t)inst * 4;
-            float m[12];
-            int root, mat;
-            load_instance(ir, m, &root, &mat);
-            const float4 e3 = ldg4(ir + 3);
-            const v3 iro = xform(m, o, 1.0f), ird = xform(m, d, 0.0f);
-            bool ofast;
-            const v3 iinvd = inv_dir(ird, &ofast);
-            code = kEmpty;
-            if (!ofast)
-            {
-                // copies, so that t and the hit record keep no address and stay in registers
-                bool anyHit = false;
-                float tm = t;
-                Hit hm = *out;
-                err |= mesh_binary<kAny>(S, root, inst, iro, ird, &tm, &hm, &anyHit, o, winvd);
-                t = tm;
-                *out = hm;
-                if (kAny && anyHit)
-                {
-                    *tBest = t;
-                    return err;
-                }
-            }
-            else
-            {
-                if (sp >= kWideStack) { err |= LF_DEVERR_STACK; break; }
-                stack[sp++] = kBlasEnd;
-                ro = iro;
-                rd = ird;
-                invd = iinvd;
-                meshLevel = true;
-                curInst = inst;
-                code = __float_as_int(e3.z);
-            }
-        }
-        if (code == kEmpty)
-        {
-            if (sp == 0) break;
-            code = stack[--sp];
-            if (code == kBlasEnd)
-            {
-                // leave the instance; the entry below the marker is an instance-level one
-                meshLevel = false;
-                ro = o;
-                rd = d;
-                invd = winvd;
-                if (sp == 0) break;
-                code = stack[--sp];
-            }
-        }
-    }
-    *tBest = t;
-    return err;
+    wide_init(S, w, o, d, winvd, *tBest);
+    Hit h = *out;
+    while (!wide_step<kAny>(S, w, stack, h)) {}
+    *out = h;
+    *tBest = w.t;
+    return w.err;
 }
 
 // Closest hit: analytic lights first (closest_hit.glsl:13-67), then the BVH.

@@ -148,7 +148,9 @@ __global__ void __launch_bounds__(128) trace_persistent_kernel(DevScene S, const
 }
 
 // Wide-tree form: each lane traces its ray to completion; warps take rays 32 at a time from a
-// global counter (in `perm` order), so a warp that finished early takes more work.
+// global counter (in `perm` order), so a warp that finished early takes more work. (Refilling
+// single lanes as their rays end, with the traversal state kept in registers, measured 35 %
+// slower: the binned rays of a warp stop sharing nodes and the refill logic spills.)
 template <bool kAny>
 __global__ void __launch_bounds__(128) trace_fetch_wide_kernel(DevScene S, const float4* rays, const int* perm,
                                                                long long n, int4* hits, uint8_t* occluded, int lights,
