@@ -452,6 +452,16 @@ void make_light(const float* l15, DevLight& d)
     d.vs[0] = vs.x; d.vs[1] = vs.y; d.vs[2] = vs.z;
 }
 
+// Instance-level root box (the ray-binning grid of the batched queries).
+void set_bounds(lf_scene* sc, const RefNode& root)
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        sc->boundsLo[k] = root.bmin[k];
+        sc->boundsHi[k] = root.bmax[k];
+    }
+}
+
 lf_status encode_instances(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, std::vector<float4>& recs,
                            std::vector<int>& map, std::vector<float4>& inst, std::vector<ShadeInstance>& sinst,
                            int* tlasRoot)
@@ -696,11 +706,7 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     }
     sc->numRefNodes = v->num_nodes;
     sc->topLevelIndex = v->top_level_index;
-    for (int k = 0; k < 3; ++k)
-    {
-        sc->boundsLo[k] = nodes[v->top_level_index].bmin[k];
-        sc->boundsHi[k] = nodes[v->top_level_index].bmax[k];
-    }
+    set_bounds(sc, nodes[v->top_level_index]);
     sc->d_nodes = d_nodes;
     sc->nodeCapacity = recs.size() / 4;
     sc->d_wide = d_wide;
@@ -762,6 +768,7 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     sc->view.trav.root = tlasRoot;
     sc->view.trav.numNodes = (int)(recs.size() / 4);
     sc->view.trav.wroot = wroot;
+    set_bounds(sc, nodes[v->top_level_index]);
     return LF_OK;
 }
 
