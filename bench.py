@@ -261,7 +261,7 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
     if tune:
         from lavaframe_gb300 import autotune
 
-        tuned = autotune.tune(ctx, ds, p, spp=4, triangles=int(s.view().num_tris))
+        tuned = autotune.tune(ctx, ds, p, spp=spp, triangles=int(s.view().num_tris))
     f = lf.Frame(ctx, ds, p, flags)
     if spp_batch:
         f.set_batch(spp_batch)

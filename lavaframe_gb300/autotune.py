@@ -19,6 +19,7 @@ CANDIDATES = {
     "block_shadow": [64, 128, 256],
 }
 DEFAULT = {"slots": 1 << 23, "shade_threads_per_sm": 768, "block_extend": 128, "block_shadow": 128}
+MARGIN = 0.02   # a setting replaces the current one only when it is this much faster (timing noise)
 
 
 def _signature(params, spp, triangles):
@@ -51,7 +52,9 @@ def _time_render(ctx, device_scene, params, spp, repeats):
 
 def tune(ctx, device_scene, params, spp=4, repeats=2, triangles=0, cache: str | Path | None = None):
     """Tunes the engine of `ctx` for rendering `spp` samples of `params` on `device_scene` and
-    applies the best setting. Returns {"config", "seconds", "trials", "cached"}."""
+    applies the best setting. Time it with the sample count the workload renders: the share of
+    the drain at the end of a render depends on it. Returns {"config", "seconds", "trials",
+    "cached"}."""
     key = _signature(params, spp, triangles)
     store = {}
     if cache is not None and Path(cache).exists():
@@ -71,7 +74,7 @@ def tune(ctx, device_scene, params, spp=4, repeats=2, triangles=0, cache: str | 
             _apply(ctx, trial)
             t = _time_render(ctx, device_scene, params, spp, repeats)
             trials.append({"config": trial, "seconds": t})
-            if t < best:
+            if t < best * (1.0 - MARGIN):
                 best, cfg = t, trial
     _apply(ctx, cfg)
     result = {"config": cfg, "seconds": best, "trials": trials}

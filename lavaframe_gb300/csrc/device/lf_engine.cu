@@ -307,6 +307,64 @@ __global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob 
     warp_count_add(&b.ctr[2], rays);
 }
 
+// ------------------------------------------------------------------ drain
+// The last paths of a run, once no ids are left to issue: every queued path is taken through
+// its remaining bounces by one thread (extension, shade, next-event rays, in the order of the
+// step kernels) and queued as done. Per path this is the same sequence of operations the step
+// kernels perform, so results and ray counts are unchanged; what goes away is one launch
+// sequence per bounce whose length is set by the slowest ray of an almost empty pool.
+// One path from its queued extension ray to its end; returns the extension and shadow rays
+// it traced.
+__device__ __forceinline__ void drain_path(const EngineBuffers& b, const EngineJob& J, int p, unsigned long long& ext,
+                                           unsigned long long& shadowRays)
+{
+    for (int bounce = 0; bounce < 4096; ++bounce)
+    {
+        const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
+        Hit h;
+        const uint32_t err = closest_hit<false>(J.S.trav, f3(o4), f3(d4), kInfinity, J.P.useLights != 0, &h, nullptr);
+        b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
+        set_error(b.status, err);
+        ++ext;
+        bool pushExt = false, pushShadow = false;
+        ShadowRec rec;
+        shade_path(J.S, J.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
+        if (pushShadow) set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, shadowRays));
+        if (!pushExt) return;
+    }
+}
+
+template <bool kOne>
+__global__ void __launch_bounds__(128) engine_drain_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    EngineCtl* ctl = b.ctl;
+    const int n = ctl->count[parity];
+    const int* q = b.queue[parity];
+    const int lane = threadIdx.x & 31;
+    unsigned long long ext = 0, shadowRays = 0;
+    while (true)
+    {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&ctl->extendNext, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        int p = -1;
+        if (i < n)
+        {
+            p = q[i];
+            if constexpr (kOne)
+                drain_path(b, one, p, ext, shadowRays);
+            else
+                drain_path(b, b.jobs[job_of(reinterpret_cast<const int*>(b.ps.info)[4 * p + 3])], p, ext, shadowRays);
+        }
+        __syncwarp();
+        warp_push(p >= 0, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status);
+    }
+    warp_count_add(&b.ctr[1], ext);
+    warp_count_add(&b.ctr[2], shadowRays);
+}
+
 // ------------------------------------------------------------------ accumulate
 __global__ void engine_accumulate_kernel(int width, int tileW, int tileH, EnginePass Q, float4* accum, double* accum64)
 {
@@ -413,6 +471,30 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
             b, one, parity);
     engine_shadow_kernel<kOne><<<full_grid((const void*)engine_shadow_kernel<kOne>, bw, b.cap), bw, 0, st>>>(b, one);
 }
+}
+
+template <bool kOne>
+void drain_step(const EngineBuffers& b, const EngineJob& one, cudaStream_t st)
+{
+    const int BF = 256;
+    for (int parity = 0; parity < 2; ++parity)
+    {
+        engine_finish_kernel<<<full_grid((const void*)engine_finish_kernel, BF, b.cap), BF, 0, st>>>(b, parity);
+        engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, BF, b.cap), BF, 0, st>>>(
+            b, one, parity);
+        engine_reset_kernel<<<1, 1, 0, st>>>(b.ctl, parity);
+        engine_drain_kernel<kOne><<<full_grid((const void*)engine_drain_kernel<kOne>, 128, b.cap), 128, 0, st>>>(
+            b, one, parity);
+    }
+}
+
+int launch_engine_drain(const EngineBuffers& b, const EngineJob* one, cudaStream_t st)
+{
+    if (one)
+        drain_step<true>(b, *one, st);
+    else
+        drain_step<false>(b, EngineJob{}, st);
+    return (int)cudaGetLastError();
 }
 
 int launch_engine_step(const EngineBuffers& b, const EngineJob* one, int parity, cudaStream_t st)

@@ -80,6 +80,10 @@ struct EngineBuffers
 // belongs to that job and the kernels read it from their parameters (constant bank) instead
 // of the job table.
 int launch_engine_step(const EngineBuffers& b, const EngineJob* one, int parity, cudaStream_t st);
+// Drain form of a step pair, for runs with few paths left: two steps whose extend / shade /
+// shadow kernels are replaced by one kernel that runs every queued path to its end (one thread
+// per path) and queues it as done. Leaves the parity where a step pair leaves it.
+int launch_engine_drain(const EngineBuffers& b, const EngineJob* one, cudaStream_t st);
 // Pool start: every slot on the done list, marked unused.
 int launch_engine_init(const EngineBuffers& b, cudaStream_t st);
 // Publishes newly written pass descriptors: clamps the overshoot of `next` to the old total,

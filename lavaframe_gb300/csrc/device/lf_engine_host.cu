@@ -223,14 +223,14 @@ lf_status engine_publish(EngineHost* e)
     return LF_OK;
 }
 
-lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job)
+lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job, bool drain)
 {
     lf_ctx* c = e->c;
     if (!ctr) ctr = e->ownCtr;
     const unsigned gen = job >= 0 ? e->jobGen[job] : 0;
     EngineHost::Graph* hit = nullptr;
     for (auto& g : e->graphs)
-        if (g.ctr == ctr && g.job == job && g.gen == gen) hit = &g;
+        if (g.ctr == ctr && g.job == job && g.gen == gen && g.drain == drain) hit = &g;
     if (!hit)
     {
         if (e->graphs.size() >= 8) drop_graphs(e);
@@ -241,14 +241,20 @@ lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job)
         cudaGraphExec_t exec = nullptr;
         cudaError_t err = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) return cuda_fail(c, err, "engine graph capture");
-        int le = launch_engine_step(b, one, 0, c->stream);
-        le |= launch_engine_step(b, one, 1, c->stream);
+        int le = 0;
+        if (drain)
+            le = launch_engine_drain(b, one, c->stream);
+        else
+        {
+            le = launch_engine_step(b, one, 0, c->stream);
+            le |= launch_engine_step(b, one, 1, c->stream);
+        }
         err = cudaStreamEndCapture(c->stream, &g);
         if (err == cudaSuccess && le) err = (cudaError_t)le;
         if (err == cudaSuccess) err = cudaGraphInstantiate(&exec, g, 0);
         if (g) cudaGraphDestroy(g);
         if (err != cudaSuccess) return cuda_fail(c, err, "engine graph instantiate");
-        e->graphs.push_back({exec, ctr, job, gen});
+        e->graphs.push_back({exec, ctr, job, gen, drain});
         hit = &e->graphs.back();
     }
     cudaError_t err = cudaGraphLaunch(hit->exec, c->stream);
@@ -276,18 +282,21 @@ lf_status engine_drain(EngineHost* e, unsigned long long* ctr, int maxDepth, int
         8ull * ((e->total + (unsigned long long)e->b.cap - 1) / (unsigned long long)e->b.cap + 2) *
             (unsigned long long)(maxDepth + 2) + 64ull;
     unsigned long long pairs = 0;
+    bool drain = false;
     lf_status st = engine_launch_pair(e, ctr, job);
     if (st == LF_OK) st = engine_snapshot(e, 0);
     int cur = 0;
     while (st == LF_OK)
     {
-        st = engine_launch_pair(e, ctr, job);
+        st = engine_launch_pair(e, ctr, job, drain);
         if (st == LF_OK) st = engine_snapshot(e, cur ^ 1);
         if (st != LF_OK) break;
         cudaError_t err = cudaEventSynchronize(e->ev[cur]);
         if (err != cudaSuccess) return cuda_fail(c, err, "engine step");
         const EngineCtl& s = *e->h_ctl[cur];
         if (s.active == 0 && s.next >= s.total) break;
+        // once every id is issued and few paths remain, run them to their ends in one kernel
+        if (e->drainPaths > 0 && s.next >= s.total && s.active <= e->drainPaths) drain = true;
         if (++pairs * 2 > limit) return fail(c, LF_ERR_DEVICE, "engine did not drain");
         cur ^= 1;
     }

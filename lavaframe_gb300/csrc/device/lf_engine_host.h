@@ -30,8 +30,10 @@ struct EngineHost
         unsigned long long* ctr = nullptr;
         int job = -1;                   // single job baked into the kernels, -1 = job table
         unsigned gen = 0;
+        bool drain = false;             // drain form (launch_engine_drain)
     };
     std::vector<Graph> graphs;
+    long long drainPaths = 1 << 22;     // paths left at which a frame run switches to the drain form (0 = never)
 };
 
 // Engine of the context, created on first use with the default pool size.
@@ -48,7 +50,7 @@ unsigned long long engine_pass_submit(EngineHost* e, EnginePass desc);
 lf_status engine_publish(EngineHost* e);
 // Enqueues one graph launch (two steps) counting into `ctr` (nullptr: the engine's own).
 // job >= 0: every queued path belongs to that job (single-job kernels).
-lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job);
+lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job, bool drain = false);
 // Enqueues a copy of the control block and pass counters into host buffer k and records ev[k].
 lf_status engine_snapshot(EngineHost* e, int k);
 // Runs steps until every submitted path has been written out.
