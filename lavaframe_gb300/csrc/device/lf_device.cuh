@@ -54,7 +54,8 @@ struct DevLight
 // Wide nodes collapsed from the reference's binary tree (see traverse_wide): per node
 // 2 * kWide float4 = [min x | max x | min y | max y | min z | max z | child codes | child
 // reference-node indices], kWide values per group (kWide / 4 float4 each); unused slots have
-// code kWideEmpty. The width is a build option (LF_WIDE = 4 or 8).
+// code kWideEmpty and a NaN box (no slab test passes it). The width is a build option
+// (LF_WIDE = 4 or 8).
 #ifndef LF_WIDE
 #define LF_WIDE 4
 #endif
@@ -155,7 +156,8 @@ __device__ __forceinline__ bool fast_inv(float x) { return fabsf(x) < 3.0e38f &&
 // Inverse direction and whether the fast box test applies to it.
 __device__ __forceinline__ v3 inv_dir(v3 d, bool* fast)
 {
-    v3 inv = 1.0f / d;
+    // __frcp_rn is the correctly rounded reciprocal: the same bits as the IEEE division 1.0f / x
+    v3 inv(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
     *fast = fast_inv(inv.x) && fast_inv(inv.y) && fast_inv(inv.z);
     return inv;
 }
@@ -556,10 +558,13 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
     {
-        const int cdj = __float_as_int(g[6][j]);
-        float e;
-        const float h = box_hit_fast(g[0][j], g[2][j], g[4][j], g[1][j], g[3][j], g[5][j], ro, invd, &e);
-        const bool hit = cdj != kWideEmpty && h > 0.f && e <= lim;
+        // box_hit_fast's value is > 0 exactly when t1 >= t0 and t1 > 0; NaN boxes fail both
+        const float fx = (g[1][j] - ro.x) * invd.x, fy = (g[3][j] - ro.y) * invd.y, fz = (g[5][j] - ro.z) * invd.z;
+        const float nx = (g[0][j] - ro.x) * invd.x, ny = (g[2][j] - ro.y) * invd.y, nz = (g[4][j] - ro.z) * invd.z;
+        const float t1 = fmin3_hw(fmaxf(fx, nx), fmaxf(fy, ny), fmaxf(fz, nz));
+        const float t0 = fmax3_hw(fminf(fx, nx), fminf(fy, ny), fminf(fz, nz));
+        const float e = fmaxf(t0, 0.f);
+        const bool hit = t1 >= t0 && t1 > 0.f && e <= lim;
         key[j] = hit ? ((__float_as_uint(e) & ~kSlotMask) | (uint32_t)j) : 0xFFFFFFFFu;
         nh += hit ? 1 : 0;
     }

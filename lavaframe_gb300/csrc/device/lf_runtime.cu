@@ -3,6 +3,7 @@
 // render targets. Host code here must be compiled with -ffp-contract=off: light
 // precomputation and matrix inverses are part of the arithmetic contract.
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -319,7 +320,9 @@ lf_status wide_level(lf_ctx* c, WideBuilder& B, int start, bool meshLevel, int* 
         for (int j = 0; j < kWide; ++j)
         {
             int code = kWideEmpty, refIdx = -1;
-            float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+            // an unused slot gets a NaN box, which no slab test passes
+            const float qnan = std::numeric_limits<float>::quiet_NaN();
+            float lo[3] = {qnan, qnan, qnan}, hi[3] = {qnan, qnan, qnan};
             if (j < (int)kids.size())
             {
                 const int k = kids[j];
