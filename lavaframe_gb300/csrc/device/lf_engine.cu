@@ -236,8 +236,8 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
 }
 
 // Blocks of at most 256 threads. kThreadsPerSm > 0 caps registers so that many threads fit on
-// an SM (512: 128 registers, no spills; 768: 85 registers, a few spills); 0 leaves the
-// compiler's choice.
+// an SM (512: 128 registers, no spills; 768: 85 registers, a few spills; 1024: 64 registers);
+// 0 leaves the compiler's choice.
 template <bool kOne, int kThreadsPerSm>
 __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
     engine_shade_kernel(EngineBuffers b, EngineJob one, int parity)
@@ -466,6 +466,9 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
     else if (b.shadeThreadsPerSm == 768)
         engine_shade_kernel<kOne, 768><<<full_grid((const void*)engine_shade_kernel<kOne, 768>, bs, b.cap), bs, 0, st>>>(
             b, one, parity);
+    else if (b.shadeThreadsPerSm == 1024)
+        engine_shade_kernel<kOne, 1024><<<full_grid((const void*)engine_shade_kernel<kOne, 1024>, bs, b.cap), bs, 0,
+                                          st>>>(b, one, parity);
     else
         engine_shade_kernel<kOne, 0><<<full_grid((const void*)engine_shade_kernel<kOne, 0>, bs, b.cap), bs, 0, st>>>(
             b, one, parity);

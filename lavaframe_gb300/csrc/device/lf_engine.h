@@ -73,7 +73,7 @@ struct EngineBuffers
     unsigned long long* ctr;     // [1] extension rays, [2] shadow rays, [3] light-index clamps
     int cap;                     // pool slots
     int blockExtend, blockShade, blockShadow;
-    int shadeThreadsPerSm;       // register cap of the shade kernel: 0 none, 512 or 768
+    int shadeThreadsPerSm;       // register cap of the shade kernel: 0 none, 512, 768 or 1024
 };
 
 // Launches one engine step with queue parity `parity` on `st`. With `one` set, every path

@@ -12,7 +12,7 @@ namespace lfrt
 namespace
 {
 constexpr int kDefaultSlots = 1 << 23;      // ~2 GB of path state: enough rays in flight for 152 SMs
-constexpr int kDefaultShadeCap = 768;       // shade kernel register cap (threads per SM)
+constexpr int kDefaultShadeCap = 1024;      // shade kernel register cap (threads per SM)
 constexpr int kMaxJobs = 4096;
 constexpr size_t kRunRadianceBytes = size_t(2) << 30;   // radiance buffers of one frame run
 
@@ -148,7 +148,8 @@ lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockS
 {
     lf_ctx* c = e->c;
     auto okBlock = [](int b) { return b == 0 || (b >= 32 && b <= 1024 && b % 32 == 0); };
-    const bool capOk = (shadeThreadsPerSm == 0 || shadeThreadsPerSm == 512 || shadeThreadsPerSm == 768) &&
+    const bool capOk = (shadeThreadsPerSm == 0 || shadeThreadsPerSm == 512 || shadeThreadsPerSm == 768 ||
+                        shadeThreadsPerSm == 1024) &&
                        blockShade <= 256;
     if (slots < 0 || !okBlock(blockExtend) || !okBlock(blockShade) || !okBlock(blockShadow) || !capOk)
         return fail(c, LF_ERR_INVALID, "engine configuration out of range");

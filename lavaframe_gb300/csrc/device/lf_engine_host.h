@@ -39,7 +39,7 @@ struct EngineHost
 // Engine of the context, created on first use with the default pool size.
 lf_status engine_get(lf_ctx* c, EngineHost** out);
 // Pool slots (0 keeps the current pool), block sizes of extend / shade / shadow (0 = default)
-// and the register cap of shade (threads per SM it must fit: 0 none, 512, 768).
+// and the register cap of shade (threads per SM it must fit: 0 none, 512, 768, 1024).
 lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockShade, int blockShadow,
                            int shadeThreadsPerSm);
 int engine_job_alloc(EngineHost* e, const ShadeScene& S, const Params& P);

@@ -14,7 +14,7 @@ from tests import scenes
 pytestmark = pytest.mark.gpu
 
 DEFAULT_SLOTS = 1 << 23
-DEFAULT_SHADE_CAP = 768
+DEFAULT_SHADE_CAP = 1024
 
 
 def icospheres():
