@@ -51,14 +51,22 @@ __global__ void generate_kernel(ShadeScene S, Params P, PathSoA ps, int firstSam
 }
 
 // ------------------------------------------------------------------ extend
-__global__ void extend_kernel(ShadeScene S, Params P, PathSoA ps, const int* queue, const int* qcount,
-                              uint32_t* status, unsigned long long* ctr)
+// Warps take queue entries 32 at a time from `fetch`; 72 registers (7 blocks of 128 per SM).
+__global__ void __maxnreg__(72) extend_kernel(ShadeScene S, Params P, PathSoA ps, const int* queue, const int* qcount,
+                                              unsigned long long* fetch, uint32_t* status, unsigned long long* ctr)
 {
     const int n = *qcount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr[1], (unsigned long long)n);
     const bool lights = P.useLights != 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    const int lane = threadIdx.x & 31;
+    while (true)
     {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const int i = (int)base + lane;
+        if (i >= n) continue;
         int p = queue[i];
         float4 o4 = ps.o[p], d4 = ps.d[p];
         Hit h;
@@ -96,13 +104,22 @@ __global__ void __launch_bounds__(128, 4) shade_kernel(ShadeScene S, Params P, P
 }
 
 // ------------------------------------------------------------------ shadow
-__global__ void shadow_kernel(ShadeScene S, Params P, PathSoA ps, const ShadowRec* sq, const int* sqCount,
-                              uint32_t* status, unsigned long long* ctr)
+__global__ void __maxnreg__(72) shadow_kernel(ShadeScene S, Params P, PathSoA ps, const ShadowRec* sq,
+                                              const int* sqCount, unsigned long long* fetch, uint32_t* status,
+                                              unsigned long long* ctr)
 {
     const int n = *sqCount;
     unsigned long long rays = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        set_error(status, shadow_path(S, P, ps, sq[i], rays));
+    const int lane = threadIdx.x & 31;
+    while (true)
+    {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const int i = (int)base + lane;
+        if (i < n) set_error(status, shadow_path(S, P, ps, sq[i], rays));
+    }
     warp_count_add(&ctr[2], rays);
 }
 
@@ -461,20 +478,20 @@ int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const
     cudaMemsetAsync(cout, 0, sizeof(int), st);
     cudaMemsetAsync(b.shadowCount, 0, sizeof(int), st);
     const int BE = 128, BS = 128, BW = 128;
-    if (b.fetch)
+    cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
+    if (b.persistent)
     {
-        cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
         int ge = grid_for((const void*)extend_persistent_kernel, BE, cap);
         extend_persistent_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
     }
     else
     {
         int ge = grid_for((const void*)extend_kernel, BE, cap);
-        extend_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.status, b.ctr);
+        extend_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
     }
     int gs = grid_for((const void*)shade_kernel, BS, cap);
     shade_kernel<<<gs, BS, 0, st>>>(S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr);
-    if (b.fetch)
+    if (b.persistent)
     {
         int gw = grid_for((const void*)shadow_persistent_kernel, BW, cap);
         shadow_persistent_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
@@ -482,7 +499,7 @@ int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const
     else
     {
         int gw = grid_for((const void*)shadow_kernel, BW, cap);
-        shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.status, b.ctr);
+        shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
     }
     return (int)cudaGetLastError();
 }
@@ -497,7 +514,9 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
     cudaMemsetAsync(cout, 0, sizeof(int), st);
     cudaMemsetAsync(b.shadowCount, 0, sizeof(int), st);
     const int B = 128;
-    extend_kernel<<<grid_for((const void*)extend_kernel, B, cap), B, 0, st>>>(S, P, ps, qin, cin, b.status, b.ctr);
+    cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
+    extend_kernel<<<grid_for((const void*)extend_kernel, B, cap), B, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status,
+                                                                              b.ctr);
     guide_query_kernel<<<grid_for((const void*)guide_query_kernel, B, cap), B, 0, st>>>(S, ps, qin, cin, g.queries);
     int e = guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
     if (e) return e;
@@ -505,7 +524,7 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
     shade_guided_kernel<<<grid_for((const void*)shade_guided_kernel, B, cap), B, 0, st>>>(
         S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr, gc);
     shadow_kernel<<<grid_for((const void*)shadow_kernel, B, cap), B, 0, st>>>(S, P, ps, b.shadow, b.shadowCount,
-                                                                             b.status, b.ctr);
+                                                                             b.fetch + 1, b.status, b.ctr);
     return (int)cudaGetLastError();
 }
 
