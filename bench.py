@@ -549,11 +549,15 @@ def main():
                 if line.startswith("dram_bytes_per_ray:"):
                     traffic = float(line.split(":")[1].split()[0]) * nrays
         if not args.no_extras:
-            for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8)):
+            for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8), ("c3_1m_autotuned", 0)):
                 try:
-                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags, tune=(w == "c3_1m"))
+                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags,
+                                            tune=(w == "c3_1m_autotuned"))
                 except Exception as e:  # reported, not fatal for the headline
                     extra[w] = {"error": str(e)}
+            from lavaframe_gb300 import autotune
+
+            autotune.apply_default(ctx)   # the remaining workloads run on the default engine
             for w, fn in (("c4_guiding_640x360", lambda: run_guiding(ctx, 640, 360, 4096)),
                           ("c5_serving_16_jobs", lambda: run_serving(ctx, 16, max_spp=64))):
                 try:

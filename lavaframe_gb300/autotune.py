@@ -9,7 +9,6 @@ signature (resolution, samples, depth, triangles).
 from __future__ import annotations
 
 import json
-import time
 from pathlib import Path
 
 CANDIDATES = {
@@ -31,7 +30,14 @@ def _apply(ctx, cfg):
                          block_shadow=cfg["block_shadow"], shade_threads_per_sm=cfg["shade_threads_per_sm"])
 
 
+def apply_default(ctx):
+    """Puts the engine of `ctx` back on the default setting."""
+    _apply(ctx, DEFAULT)
+
+
 def _time_render(ctx, device_scene, params, spp, repeats):
+    """Best device time (CUDA events on the context's stream) of `repeats` renders of `spp`
+    samples, after a one-sample warm-up render."""
     import lavaframe_gb300 as lf
 
     f = lf.Frame(ctx, device_scene, params)
@@ -41,16 +47,17 @@ def _time_render(ctx, device_scene, params, spp, repeats):
         best = float("inf")
         for r in range(repeats):
             f.reset()
-            t0 = time.perf_counter()
+            ctx.timer_start()
             f.render(1 + r * spp, spp)
+            ms = ctx.timer_stop()
             f.sync()
-            best = min(best, time.perf_counter() - t0)
+            best = min(best, ms / 1e3)
     finally:
         f.close()
     return best
 
 
-def tune(ctx, device_scene, params, spp=4, repeats=2, triangles=0, cache: str | Path | None = None):
+def tune(ctx, device_scene, params, spp=4, repeats=3, triangles=0, cache: str | Path | None = None):
     """Tunes the engine of `ctx` for rendering `spp` samples of `params` on `device_scene` and
     applies the best setting. Time it with the sample count the workload renders: the share of
     the drain at the end of a render depends on it. Returns {"config", "seconds", "trials",

@@ -76,7 +76,7 @@ __global__ void engine_init_kernel(EngineBuffers b)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
     {
         b.ps.info[i] = make_int4(0, 0, 0, -1);
-        b.freeList[i] = i;
+        b.freeList[b.cap - 1 - i] = i;   // refill takes from the top: slot 0 first
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
@@ -89,6 +89,18 @@ __global__ void engine_init_kernel(EngineBuffers b)
         b.ctl->count[1] = 0;
         b.ctl->shadowCount = 0;
     }
+}
+
+// With the pool idle (every slot free, no path active), puts the free list back in slot order:
+// finished paths return their slots in completion order, and over many runs new paths would
+// otherwise take scattered slots, so that the 32 paths of a warp read their state from 32
+// different cache lines instead of a few.
+__global__ void engine_order_free_kernel(EngineBuffers b)
+{
+    const EngineCtl* c = b.ctl;
+    if (c->freeCount != b.cap || c->active != 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
+        b.freeList[b.cap - 1 - i] = i;   // refill takes from the top: slot 0 first
 }
 
 __global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, unsigned long long numPasses)
@@ -441,6 +453,7 @@ int launch_engine_init(const EngineBuffers& b, cudaStream_t st)
 int launch_engine_append(const EngineBuffers& b, unsigned long long total, unsigned long long numPasses,
                          cudaStream_t st)
 {
+    engine_order_free_kernel<<<full_grid((const void*)engine_order_free_kernel, 256, b.cap), 256, 0, st>>>(b);
     engine_append_kernel<<<1, 1, 0, st>>>(b, total, numPasses);
     return (int)cudaGetLastError();
 }
