@@ -75,8 +75,7 @@ __global__ void engine_init_kernel(EngineBuffers b)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
     {
-        b.ps.info[i] = make_int4(0, 0, 0, -1);
-        b.freeList[b.cap - 1 - i] = i;   // refill takes from the top: slot 0 first
+        b.ps.info[i] = make_int4(0, 0, 0, -1);   // info.w = -1: the slot is free
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
@@ -89,18 +88,6 @@ __global__ void engine_init_kernel(EngineBuffers b)
         b.ctl->count[1] = 0;
         b.ctl->shadowCount = 0;
     }
-}
-
-// With the pool idle (every slot free, no path active), puts the free list back in slot order:
-// finished paths return their slots in completion order, and over many runs new paths would
-// otherwise take scattered slots, so that the 32 paths of a warp read their state from 32
-// different cache lines instead of a few.
-__global__ void engine_order_free_kernel(EngineBuffers b)
-{
-    const EngineCtl* c = b.ctl;
-    if (c->freeCount != b.cap || c->active != 0) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.cap; i += gridDim.x * blockDim.x)
-        b.freeList[b.cap - 1 - i] = i;   // refill takes from the top: slot 0 first
 }
 
 __global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, unsigned long long numPasses)
@@ -133,11 +120,12 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
     c->extendNext = 0;
     c->shadeNext = 0;
     c->shadowNext = 0;
+    c->refillNext = 0;
 }
 
 // ------------------------------------------------------------------ finish / refill
 // Writes out the radiance of every path that finished in the previous step (counting pass
-// completions) and returns its slot to the free list.
+// completions) and frees its slot.
 __global__ void engine_finish_kernel(EngineBuffers b, int parity)
 {
     __shared__ int smem[33];
@@ -160,19 +148,27 @@ __global__ void engine_finish_kernel(EngineBuffers b, int parity)
             info[3] = -1;
         }
         count_done_block(ring, b.passDone, table);
-        block_push(slot >= 0, slot, b.freeList, &ctl->freeCount, b.cap, b.status, smem);
         const int written = __popc(__ballot_sync(kFull, ring >= 0));
-        if (lane == 0 && written) atomicSub(&ctl->active, written);
+        if (lane == 0 && written)
+        {
+            atomicSub(&ctl->active, written);
+            atomicAdd(&ctl->freeCount, written);
+        }
     }
 }
 
-// Starts min(free slots, unissued ids) new paths: the k-th one takes id next + k and the k-th
-// slot from the top of the free list, gets its camera ray (renderer.glsl:27-62) and is queued
-// for extension (a depth-0 job's paths go straight to the done list with zero radiance).
+// Starts min(free slots, unissued ids) new paths in free slots taken in slot order: the pool is
+// scanned block by block, a block's free slots get consecutive ids (next + k for the k-th slot
+// handed out), each new path gets its camera ray (renderer.glsl:27-62) and is queued for
+// extension (a depth-0 job's paths go straight to the done list with zero radiance). Handing
+// out slots in slot order keeps the paths a warp shades in neighbouring slots, so their state
+// comes in few cache lines, however the earlier paths finished.
 template <bool kOne>
 __global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
 {
     __shared__ int smem[33];
+    __shared__ int warpFree[32];
+    __shared__ int blockBase, blockDone;
     EngineCtl* ctl = b.ctl;
     const unsigned long long next = ctl->next, total = ctl->total;
     const int freeCount = ctl->freeCount;
@@ -182,14 +178,38 @@ __global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->taken = m;
     const unsigned long long plo = ctl->passLo, phi = ctl->numPasses;
     const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x; base < m; base += stride)   // block-uniform
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int base = blockIdx.x * blockDim.x; base < b.cap; base += stride)   // block-uniform
     {
-        const int k = base + threadIdx.x;
+        const int cand = base + threadIdx.x;
+        const bool isFree = cand < b.cap && reinterpret_cast<const int*>(b.ps.info)[4 * cand + 3] == -1;
+        // rank of this free slot in the block, and the block's first id offset
+        const unsigned fm = __ballot_sync(kFull, isFree);
+        if (lane == 0) warpFree[warp] = __popc(fm);
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            int tot = 0;
+            for (int w = 0; w < nw; ++w)
+            {
+                const int c = warpFree[w];
+                warpFree[w] = tot;
+                tot += c;
+            }
+            // ids handed out so far: this block's share, or a look at the counter
+            blockBase = atomicAdd(&ctl->refillNext, tot);
+            blockDone = blockBase >= m;
+        }
+        __syncthreads();
+        const int k = blockBase + warpFree[warp] + __popc(fm & ((1u << lane) - 1u));
+        const bool stop = blockDone;
+        __syncthreads();
+        if (stop) break;   // every id of this step is handed out
         int slot = -1;
         bool run = false;
-        if (k < m)
+        if (isFree && k < m)
         {
-            slot = b.freeList[freeCount - 1 - k];
+            slot = cand;
             const unsigned long long id = next + (unsigned long long)k;
             const unsigned long long g = find_pass(b.passes, id, plo, phi);
             const int r = (int)(g & (kPassRing - 1));
@@ -453,7 +473,6 @@ int launch_engine_init(const EngineBuffers& b, cudaStream_t st)
 int launch_engine_append(const EngineBuffers& b, unsigned long long total, unsigned long long numPasses,
                          cudaStream_t st)
 {
-    engine_order_free_kernel<<<full_grid((const void*)engine_order_free_kernel, 256, b.cap), 256, 0, st>>>(b);
     engine_append_kernel<<<1, 1, 0, st>>>(b, total, numPasses);
     return (int)cudaGetLastError();
 }

@@ -53,9 +53,10 @@ struct EngineCtl
     int shadowCount;
     int doneCount[2];              // done-list sizes
     int active;                    // paths started and not yet written out
-    int freeCount;                 // slots on the free list
+    int freeCount;                 // free slots (info.w == -1)
     int taken;                     // slots the current step's refill started
     int extendNext, shadeNext, shadowNext;   // work counters of the extend, shade and shadow kernels
+    int refillNext;                // ids handed out by the current refill
 };
 
 struct EngineBuffers
@@ -64,7 +65,6 @@ struct EngineBuffers
     int* queue[2];
     ShadowRec* shadow;
     int* done[2];                // slots whose path finished
-    int* freeList;               // slots without a path (a stack)
     EngineCtl* ctl;
     const EngineJob* jobs;
     const EnginePass* passes;    // ring of kPassRing

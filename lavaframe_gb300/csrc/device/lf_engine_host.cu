@@ -52,7 +52,6 @@ lf_status alloc_pool(EngineHost* e, int slots)
     A(&b.queue[1], slots);
     A(&b.done[0], slots);
     A(&b.done[1], slots);
-    A(&b.freeList, slots);
     A(&b.shadow, slots);
     if (err != cudaSuccess)
     {
