@@ -13,7 +13,7 @@ from tests import scenes
 
 pytestmark = pytest.mark.gpu
 
-DEFAULT_SLOTS = 1 << 23
+DEFAULT_SLOTS = 1 << 24
 DEFAULT_SHADE_CAP = 1024
 
 
