@@ -124,125 +124,6 @@ __global__ void __maxnreg__(72) shadow_kernel(ShadeScene S, Params P, PathSoA ps
     warp_count_add(&ctr[2], rays);
 }
 
-// ------------------------------------------------------------------ persistent extend / shadow
-// Same work as extend_kernel / shadow_kernel, organised like the batched ray queries: warps
-// stay resident, and a lane whose ray finished takes the next queue entry (one atomic per
-// warp refill), so long rays do not hold a whole warp of finished lanes.
-__global__ void __launch_bounds__(128) extend_persistent_kernel(ShadeScene S, Params P, PathSoA ps, const int* queue,
-                                                                 const int* qcount, unsigned long long* fetch,
-                                                                 uint32_t* status, unsigned long long* ctr)
-{
-    const int n = *qcount;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr[1], (unsigned long long)n);
-    const int lane = threadIdx.x & 31;
-    TravState s;
-    int p = -1;          // -1: needs work, -2: queue exhausted
-    int light = -1;
-    while (true)
-    {
-        unsigned need = __ballot_sync(kFull, p == -1);
-        if (need)
-        {
-            int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(need));
-            base = __shfl_sync(kFull, base, leader);
-            if (p == -1)
-            {
-                unsigned long long my = base + __popc(need & ((1u << lane) - 1u));
-                if (my < (unsigned long long)n)
-                {
-                    p = queue[my];
-                    v3 o = f3(ps.o[p]), d = f3(ps.d[p]);
-                    float t = kInfinity;
-                    light = -1;
-                    if (P.useLights) t = lights_closest(S.trav, o, d, t, &light);
-                    trav_init(s, S.trav, o, d, t);
-                }
-                else
-                    p = -2;
-            }
-        }
-        if (__all_sync(kFull, p == -2)) break;
-        if (p >= 0 && trav_run<false>(s, S.trav, 32))
-        {
-            ps.hit[p] = make_float4(s.t, __int_as_float(s.hitInst), __int_as_float(s.hitPrim),
-                                    __int_as_float(s.hitPrim >= 0 ? -1 : light));
-            set_error(status, s.err);
-            p = -1;
-        }
-    }
-}
-
-__global__ void __launch_bounds__(128) shadow_persistent_kernel(ShadeScene S, Params P, PathSoA ps, const ShadowRec* sq,
-                                                                 const int* sqCount, unsigned long long* fetch,
-                                                                 uint32_t* status, unsigned long long* ctr)
-{
-    const int n = *sqCount;
-    const int lane = threadIdx.x & 31;
-    TravState s;
-    int r = -1;          // record index; -1: needs work, -2: exhausted
-    int phase = 0;       // 0: environment ray, 1: light ray, 2: done
-    bool tracing = false;
-    v3 Li(0.0f);
-    unsigned long long rays = 0;
-    while (true)
-    {
-        unsigned need = __ballot_sync(kFull, r == -1);
-        if (need)
-        {
-            int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(fetch, (unsigned long long)__popc(need));
-            base = __shfl_sync(kFull, base, leader);
-            if (r == -1)
-            {
-                unsigned long long my = base + __popc(need & ((1u << lane) - 1u));
-                r = my < (unsigned long long)n ? (int)my : -2;
-                phase = 0;
-                tracing = false;
-                Li = v3(0.0f);
-            }
-        }
-        if (__all_sync(kFull, r == -2)) break;
-        if (r < 0) continue;
-        if (!tracing)
-        {
-            const uint32_t flags = __float_as_uint(sq[r].b.w);
-            while (phase < 2 && !(flags & (1u << phase))) ++phase;
-            if (phase == 2)
-            {
-                // DirectLight's Li, then radiance += Li * throughput (pathtrace.glsl:266)
-                const int p = __float_as_int(sq[r].a.w);
-                v3 L = f3(ps.L[p]) + Li * f3(sq[r].b);
-                ps.L[p] = f4(L, 0.f);
-                r = -1;
-                continue;
-            }
-            const v3 pos = f3(sq[r].a);
-            const float4 dir4 = phase == 0 ? sq[r].c : sq[r].f;
-            const float maxd = phase == 0 ? kInfinity - kEps : sq[r].f.w;
-            const v3 dir = f3(dir4);
-            ++rays;
-            if (P.useLights && lights_any(S.trav, pos, dir, maxd))
-            {
-                ++phase;   // occluded by an analytic light
-                continue;
-            }
-            trav_init(s, S.trav, pos, dir, maxd);
-            tracing = true;
-        }
-        if (trav_run<true>(s, S.trav, 32))
-        {
-            if (s.hitPrim < 0) Li = Li + (phase == 0 ? f3(sq[r].e) : f3(sq[r].g));
-            set_error(status, s.err);
-            tracing = false;
-            ++phase;
-        }
-    }
-    warp_count_add(&ctr[2], rays);
-}
-
 // ------------------------------------------------------------------ accumulate
 __global__ void accumulate_kernel(Params P, PathSoA ps, int nSamples, float4* accum, double* accum64)
 {
@@ -480,28 +361,12 @@ int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const
     cudaMemsetAsync(b.shadowCount, 0, sizeof(int), st);
     const int BE = 128, BS = 128, BW = 128;
     cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
-    if (b.persistent)
-    {
-        int ge = grid_for((const void*)extend_persistent_kernel, BE, cap);
-        extend_persistent_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
-    }
-    else
-    {
-        int ge = grid_for((const void*)extend_kernel, BE, cap);
-        extend_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
-    }
+    int ge = grid_for((const void*)extend_kernel, BE, cap);
+    extend_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
     int gs = grid_for((const void*)shade_kernel, BS, cap);
     shade_kernel<<<gs, BS, 0, st>>>(S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr);
-    if (b.persistent)
-    {
-        int gw = grid_for((const void*)shadow_persistent_kernel, BW, cap);
-        shadow_persistent_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
-    }
-    else
-    {
-        int gw = grid_for((const void*)shadow_kernel, BW, cap);
-        shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
-    }
+    int gw = grid_for((const void*)shadow_kernel, BW, cap);
+    shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
     return (int)cudaGetLastError();
 }
 

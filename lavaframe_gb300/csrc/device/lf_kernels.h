@@ -41,7 +41,6 @@ struct BounceBuffers
     uint32_t* status;
     unsigned long long* ctr;   // [0] paths, [1] extension rays, [2] shadow rays, [3] light clamps
     unsigned long long* fetch; // [2] work counters of the extend / shadow kernels
-    int persistent;            // binary-tree persistent extend / shadow kernels instead
 };
 
 // Floats per recorded path vertex of guided rendering (see GuideCtx in lf_pathops.cuh).

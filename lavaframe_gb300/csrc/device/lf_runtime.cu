@@ -1160,10 +1160,7 @@ lf_status run_batch(lf_frame* f, Params P, int firstSample, int n, bool record =
                         : cuda_fail(c, (cudaError_t)e, "generate launch");
     BounceBuffers bb = f->bb;
     // Queue order is already coherent (camera rays in pixel order, survivors compacted in
-    // order): warps take 32 queued rays at a time and trace each to its end (wide tree);
-    // LF_WAVEFRONT_PERSISTENT=1 selects the binary-tree persistent kernels that refill lanes.
-    static const bool persistent = std::getenv("LF_WAVEFRONT_PERSISTENT") != nullptr;
-    bb.persistent = persistent ? 1 : 0;
+    // order): warps take 32 queued rays at a time and trace each to its end.
     if (f->guide)
     {
         GuideBuffers gb = f->gb;
@@ -1605,7 +1602,6 @@ extern "C" lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, 
     bb.status = (uint32_t*)(base + 12);
     bb.ctr = (unsigned long long*)(base + 16);
     bb.fetch = (unsigned long long*)(base + 48);
-    bb.persistent = 0;
 
     // the array keeps the previous call's contents: clear sizes, status and counters
     cudaError_t e = cudaMemsetAsync(base, 0, kNoAllocHeader, c->stream);
