@@ -454,9 +454,7 @@ int sm_count()
 
 int full_grid(const void* kernel, int block, long long work)
 {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-    if (per_sm <= 0) per_sm = 1;
+    const int per_sm = occupancy_blocks_per_sm(kernel, block);
     long long full = (long long)sm_count() * per_sm;
     long long need = (work + block - 1) / block;
     if (need < 1) need = 1;

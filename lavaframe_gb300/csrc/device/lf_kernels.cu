@@ -10,6 +10,9 @@
 // Path state lives in SoA arrays in HBM; queues are compacted with one atomic per warp
 // (ballot + popc). Every kernel runs a warp-uniform grid-stride loop over a device-side
 // count, so the bounce loop needs no host round trip and can be captured in a graph.
+#include <mutex>
+#include <vector>
+
 #include "lf_pathops.cuh"
 
 namespace lfd
@@ -330,14 +333,36 @@ int grid_for(const void* kernel, int block, long long work)
         cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_num_sms <= 0) g_num_sms = 1;
     }
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-    if (per_sm <= 0) per_sm = 1;
+    const int per_sm = occupancy_blocks_per_sm(kernel, block);
     long long full = (long long)g_num_sms * per_sm;
     long long need = (work + block - 1) / block;
     if (need < 1) need = 1;
     return (int)(need < full ? need : full);
 }
+}
+
+int occupancy_blocks_per_sm(const void* kernel, int block)
+{
+    struct Entry
+    {
+        const void* kernel;
+        int block, perSm, device;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const Entry& e : cache)
+            if (e.kernel == kernel && e.block == block && e.device == dev) return e.perSm;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (per_sm <= 0) per_sm = 1;
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back({kernel, block, per_sm, dev});
+    return per_sm;
 }
 
 int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,

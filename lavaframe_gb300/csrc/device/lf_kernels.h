@@ -67,6 +67,10 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
 // Training samples from the recorded vertices of the batch's n paths.
 int launch_guide_collect(const PathSoA& ps, const GuideBuffers& g, long long n, cudaStream_t st);
 
+// Resident blocks per SM of `kernel` at `block` threads (the occupancy query, remembered per
+// kernel and block size: the query costs more host time than a launch).
+int occupancy_blocks_per_sm(const void* kernel, int block);
+
 int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,
                     int* queue, int* qcount, cudaStream_t st);
 int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const BounceBuffers& b, int bounce,

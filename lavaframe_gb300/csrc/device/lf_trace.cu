@@ -263,13 +263,13 @@ int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void
     {
         if (any)
         {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fetch_wide_kernel<true>, 128, 0);
+            per_sm = occupancy_blocks_per_sm((const void*)trace_fetch_wide_kernel<true>, 128);
             trace_fetch_wide_kernel<true><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
                 S, rays, order, n, nullptr, (uint8_t*)out, lights, next, status);
         }
         else
         {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_fetch_wide_kernel<false>, 128, 0);
+            per_sm = occupancy_blocks_per_sm((const void*)trace_fetch_wide_kernel<false>, 128);
             trace_fetch_wide_kernel<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
                 S, rays, order, n, (int4*)out, nullptr, lights, next, status);
         }
@@ -277,13 +277,13 @@ int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void
     }
     if (any)
     {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_persistent_kernel<true>, 128, 0);
+        per_sm = occupancy_blocks_per_sm((const void*)trace_persistent_kernel<true>, 128);
         trace_persistent_kernel<true><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
             S, rays, order, n, nullptr, (uint8_t*)out, lights, next, status);
     }
     else
     {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_persistent_kernel<false>, 128, 0);
+        per_sm = occupancy_blocks_per_sm((const void*)trace_persistent_kernel<false>, 128);
         trace_persistent_kernel<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
             S, rays, order, n, (int4*)out, nullptr, lights, next, status);
     }
