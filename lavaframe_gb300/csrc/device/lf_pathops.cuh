@@ -223,14 +223,8 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
             L = L + v3(P.bg[0], P.bg[1], P.bg[2]) * T;
         else if (P.envOnMiss)
         {
-            float mis = 1.0f;
-            v3 col = env_lookup(S.env, d);
-            if (depth > 0)
-            {
-                float lightPdf = EnvPdf(S.env, d);
-                mis = powerHeuristic(bsdfPdf, lightPdf);
-            }
-            L = L + mis * col * T * S.env.multiplier;
+            const v3 mc = env_miss_term(S.env, d, depth, bsdfPdf);
+            L = L + mc * T * S.env.multiplier;
         }
         ps.L[p] = f4(L, 0.f);
     }
@@ -270,7 +264,7 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
         Onb(s.normal, s.tangent, s.bitangent);
         // ---- GetMaterialsAndTextures (pathtrace.glsl:40-123)
         s.mat = load_material(S, geo.material);
-        apply_textures(S, s, d);
+        if (has_texture_maps(s.mat)) s = apply_texture_maps(S, s, d);
         s.eta = lfc::dot(d, s.normal) < 0.0f ? (1.0f / s.mat.ior) : s.mat.ior;
         info.z = geo.material;
         const float* mix = kGuided ? gc.mix + (size_t)qpos * guide::kMixFloats : nullptr;

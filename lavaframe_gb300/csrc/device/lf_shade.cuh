@@ -351,6 +351,18 @@ __device__ __forceinline__ void apply_textures(const ShadeScene& S, Surf& s, v3 
     }
 }
 
+// Texture maps of a surface, out of line (most scenes have none; the check stays inline).
+static __device__ __noinline__ Surf apply_texture_maps(const ShadeScene S, Surf s, v3 rdir)
+{
+    apply_textures(S, s, rdir);
+    return s;
+}
+
+__device__ __forceinline__ bool has_texture_maps(const Mat& m)
+{
+    return (int)m.texIDs[0] >= 0 || (int)m.texIDs[1] >= 0 || (int)m.texIDs[2] >= 0 || m.texIDs[3] >= 0.0f;
+}
+
 // Emission of a material evaluated at a texture coordinate (texture map included).
 __device__ __forceinline__ v3 material_emission(const ShadeScene& S, int matId, v2 texCoord)
 {
@@ -579,10 +591,29 @@ __device__ __forceinline__ float EnvPdf(const EnvMap& E, v3 dir)
 }
 
 // Miss contribution before the throughput product (pathtrace.glsl:223-244).
+__device__ __forceinline__ v3 env_lookup(const EnvMap& E, v3 dir);
+
+// The environment term of a miss, mis * colour (out of line: misses are a minority of hits).
+static __device__ __noinline__ v3 env_miss_term(const EnvMap E, v3 d, int depth, float bsdfPdf);
 __device__ __forceinline__ v3 env_lookup(const EnvMap& E, v3 dir)
 {
     float ux = (kPI + lfc::atan2_c(dir.z, dir.x)) * (1.0f / kTWO_PI);
     float uy = lfc::acos_c(dir.y) * (1.0f / kPI);
     return bilinear_rgb(E.rgb, E.w, E.h, ux, uy);
+}
+}
+
+namespace lfd
+{
+static __device__ __noinline__ v3 env_miss_term(const EnvMap E, v3 d, int depth, float bsdfPdf)
+{
+    float mis = 1.0f;
+    v3 col = env_lookup(E, d);
+    if (depth > 0)
+    {
+        float lightPdf = EnvPdf(E, d);
+        mis = powerHeuristic(bsdfPdf, lightPdf);
+    }
+    return mis * col;
 }
 }
