@@ -270,7 +270,8 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
 // Blocks of at most 256 threads. kThreadsPerSm > 0 caps registers so that many threads fit on
 // an SM (512: 128 registers, no spills; 768: 85 registers, a few spills; 1024: 64 registers);
 // 0 leaves the compiler's choice.
-template <bool kOne, int kThreadsPerSm>
+// kLights = false: the job's scene has no analytic lights (single-job steps only).
+template <bool kOne, int kThreadsPerSm, bool kLights = true>
 __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
     engine_shade_kernel(EngineBuffers b, EngineJob one, int parity)
 {
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
         {
             p = qin[i];
             if constexpr (kOne)
-                shade_path(one.S, one.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
+                shade_path<kLights>(one.S, one.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
             else
             {
                 const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
@@ -496,6 +497,9 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
     else if (b.shadeThreadsPerSm == 768)
         engine_shade_kernel<kOne, 768><<<full_grid((const void*)engine_shade_kernel<kOne, 768>, bs, b.cap), bs, 0, st>>>(
             b, one, parity);
+    else if (b.shadeThreadsPerSm == 1024 && kOne && !one.P.useLights)
+        engine_shade_kernel<kOne, 1024, false><<<full_grid((const void*)engine_shade_kernel<kOne, 1024, false>, bs, b.cap),
+                                                 bs, 0, st>>>(b, one, parity);
     else if (b.shadeThreadsPerSm == 1024)
         engine_shade_kernel<kOne, 1024><<<full_grid((const void*)engine_shade_kernel<kOne, 1024>, bs, b.cap), bs, 0,
                                           st>>>(b, one, parity);

@@ -82,6 +82,7 @@ __global__ void __maxnreg__(72) extend_kernel(ShadeScene S, Params P, PathSoA ps
 // ------------------------------------------------------------------ shade
 // 8 blocks of 128 threads per SM: caps registers at 64 (some spills; 9 % faster on the 1M-
 // triangle render than 128 registers without spills).
+template <bool kLights>
 __global__ void __launch_bounds__(128, 8) shade_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin,
                                                         const int* qinCount, int* qout, int* qoutCount, ShadowRec* sq,
                                                         int* sqCount, int cap, uint32_t* status,
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(ShadeScene S, Params P, P
         if (i < n)
         {
             p = qin[i];
-            shade_path(S, P, ps, p, ctr, pushExt, pushShadow, rec);
+            shade_path<kLights>(S, P, ps, p, ctr, pushExt, pushShadow, rec);
         }
         warp_push(pushExt, p, qout, qoutCount, cap, status);
         warp_push(pushShadow, rec, sq, sqCount, cap, status);
@@ -388,8 +389,18 @@ int launch_bounce(const ShadeScene& S, const Params& P, const PathSoA& ps, const
     cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
     int ge = grid_for((const void*)extend_kernel, BE, cap);
     extend_kernel<<<ge, BE, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status, b.ctr);
-    int gs = grid_for((const void*)shade_kernel, BS, cap);
-    shade_kernel<<<gs, BS, 0, st>>>(S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr);
+    if (P.useLights)
+    {
+        int gs = grid_for((const void*)shade_kernel<true>, BS, cap);
+        shade_kernel<true><<<gs, BS, 0, st>>>(S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status,
+                                              b.ctr);
+    }
+    else
+    {
+        int gs = grid_for((const void*)shade_kernel<false>, BS, cap);
+        shade_kernel<false><<<gs, BS, 0, st>>>(S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap,
+                                               b.status, b.ctr);
+    }
     int gw = grid_for((const void*)shadow_kernel, BW, cap);
     shadow_kernel<<<gw, BW, 0, st>>>(S, P, ps, b.shadow, b.shadowCount, b.fetch + 1, b.status, b.ctr);
     return (int)cudaGetLastError();

@@ -191,7 +191,9 @@ struct GuideCtx
 // otherwise (one-sample MIS: the pdf is alpha * p_mix + (1 - alpha) * p_bsdf, the BSDF value
 // DisneyEval's), the same combined pdf weighs next-event estimation, and the vertex is
 // recorded for training; qpos is the path's queue position (index of its mixture).
-template <bool kGuided>
+// kLights = false compiles the analytic-light code out, for scenes without lights (no ray can
+// then hit a light, and next-event estimation samples the environment only).
+template <bool kGuided, bool kLights = true>
 __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
                                              unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec,
                                              const GuideCtx& gc, int qpos)
@@ -228,7 +230,7 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
         }
         ps.L[p] = f4(L, 0.f);
     }
-    else if (light >= 0)
+    else if (kLights && light >= 0)
     {
         // Analytic light: the shader still adds the emission of the material held
         // in the (stale) state from the last triangle hit before EmitterSample.
@@ -302,7 +304,7 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
                 }
             }
         }
-        if (P.useLights)
+        if (kLights && P.useLights)
         {
             const int nl = S.trav.numLights;
             int li = (int)(rnd(rng) * (float)nl);
@@ -426,10 +428,11 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
     }
 }
 
+template <bool kLights = true>
 __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
                                            unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec)
 {
-    shade_path_t<false>(S, P, ps, p, ctr, pushExt, pushShadow, rec, GuideCtx{nullptr, nullptr, 0.f, 0}, 0);
+    shade_path_t<false, kLights>(S, P, ps, p, ctr, pushExt, pushShadow, rec, GuideCtx{nullptr, nullptr, 0.f, 0}, 0);
 }
 
 // Visibility of a path's next-event rays, then radiance += Li * throughput
