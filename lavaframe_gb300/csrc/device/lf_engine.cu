@@ -106,8 +106,8 @@ __global__ void engine_append_kernel(EngineBuffers b, unsigned long long total, 
     c->passLo = lo;
 }
 
-// After finish and refill: take the refilled slots off the free list and the ids off the
-// pool of unissued paths, and clear the lists the rest of the step refills.
+// After finish and refill: count the refilled slots as taken and their ids as issued, and
+// clear the lists and counters the rest of the step fills.
 __global__ void engine_reset_kernel(EngineCtl* c, int parity)
 {
     c->freeCount -= c->taken;
