@@ -342,12 +342,13 @@ int grid_for(const void* kernel, int block, long long work)
 }
 }
 
-int occupancy_blocks_per_sm(const void* kernel, int block)
+int occupancy_blocks_per_sm(const void* kernel, int block, size_t dynamicSmem)
 {
     struct Entry
     {
         const void* kernel;
         int block, perSm, device;
+        size_t smem;
     };
     static std::mutex mu;
     static std::vector<Entry> cache;
@@ -356,13 +357,13 @@ int occupancy_blocks_per_sm(const void* kernel, int block)
     {
         std::lock_guard<std::mutex> lk(mu);
         for (const Entry& e : cache)
-            if (e.kernel == kernel && e.block == block && e.device == dev) return e.perSm;
+            if (e.kernel == kernel && e.block == block && e.device == dev && e.smem == dynamicSmem) return e.perSm;
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, dynamicSmem);
     if (per_sm <= 0) per_sm = 1;
     std::lock_guard<std::mutex> lk(mu);
-    cache.push_back({kernel, block, per_sm, dev});
+    cache.push_back({kernel, block, per_sm, dev, dynamicSmem});
     return per_sm;
 }
 

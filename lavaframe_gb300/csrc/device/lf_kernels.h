@@ -69,7 +69,7 @@ int launch_guide_collect(const PathSoA& ps, const GuideBuffers& g, long long n, 
 
 // Resident blocks per SM of `kernel` at `block` threads (the occupancy query, remembered per
 // kernel and block size: the query costs more host time than a launch).
-int occupancy_blocks_per_sm(const void* kernel, int block);
+int occupancy_blocks_per_sm(const void* kernel, int block, size_t dynamicSmem = 0);
 
 int launch_generate(const ShadeScene& S, const Params& P, const PathSoA& ps, int firstSample, int nSamples,
                     int* queue, int* qcount, cudaStream_t st);
