@@ -1,6 +1,7 @@
 // C ABI over the host scene layer (LavaFrame::Scene and LoadSceneFromFile) and the
 // procedural workload generators. Generators use only IEEE basic operations and the
 // contract functions (lf_contract.h) so they produce the same bits on every host.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -644,22 +645,48 @@ lf_status lf_gen_room(lf_hscene* s, int32_t boxes, uint64_t seed)
     sc.AddMeshInstance(MeshInstance("room", shell, Mat4(), white));
 
     SplitMix r(seed);
+    struct Box
+    {
+        v3 lo, hi;
+    };
+    std::vector<Box> all((size_t)boxes);
+    for (int b = 0; b < boxes; ++b)
+    {
+        // small clutter (2-14 cm wide, up to 30 cm high), so that 200k triangles leave the
+        // room navigable for light entering through the doorway
+        float sx = 0.02f + 0.12f * r.uniform(), sy = 0.02f + 0.28f * r.uniform(), sz = 0.02f + 0.12f * r.uniform();
+        float x = 0.3f + (9.4f - sx) * r.uniform(), z = 0.3f + (9.4f - sz) * r.uniform();
+        if (x > 8.0f && z > 3.5f && z < 6.5f) x = x - 7.5f;   // keep the way to the doorway clear
+        float y = r.uniform() < 0.9f ? 0.0f : 0.3f + 3.0f * r.uniform();
+        all[(size_t)b] = {v3(x, y, z), v3(x + sx, y + sy, z + sz)};
+    }
+    // Meshes of at most 512 boxes. Beyond one mesh, boxes are grouped by floor position (Morton
+    // order of a 64 x 64 grid over the room), so every furniture mesh covers a compact patch of
+    // floor instead of the whole room.
     const int perMesh = 512;
+    if (boxes > perMesh)
+    {
+        auto key = [](const Box& bx) {
+            auto cell = [](float c) {
+                int q = (int)(c * (64.0f / 10.0f));
+                return (uint32_t)(q < 0 ? 0 : (q > 63 ? 63 : q));
+            };
+            auto spread = [](uint32_t x) {
+                x = (x | (x << 4)) & 0x0F0Fu;
+                x = (x | (x << 2)) & 0x3333u;
+                x = (x | (x << 1)) & 0x5555u;
+                return x;
+            };
+            return (spread(cell(bx.lo.x)) << 1) | spread(cell(bx.lo.z));
+        };
+        std::stable_sort(all.begin(), all.end(), [&](const Box& a, const Box& b) { return key(a) < key(b); });
+    }
     for (int b0 = 0; b0 < boxes; b0 += perMesh)
     {
         v.clear();
         n.clear();
         int nb = boxes - b0 < perMesh ? boxes - b0 : perMesh;
-        for (int b = 0; b < nb; ++b)
-        {
-            // small clutter (2-14 cm wide, up to 30 cm high), so that 200k triangles leave the
-            // room navigable for light entering through the doorway
-            float sx = 0.02f + 0.12f * r.uniform(), sy = 0.02f + 0.28f * r.uniform(), sz = 0.02f + 0.12f * r.uniform();
-            float x = 0.3f + (9.4f - sx) * r.uniform(), z = 0.3f + (9.4f - sz) * r.uniform();
-            if (x > 8.0f && z > 3.5f && z < 6.5f) x = x - 7.5f;   // keep the way to the doorway clear
-            float y = r.uniform() < 0.9f ? 0.0f : 0.3f + 3.0f * r.uniform();
-            push_box(v, n, v3(x, y, z), v3(x + sx, y + sy, z + sz));
-        }
+        for (int b = 0; b < nb; ++b) push_box(v, n, all[(size_t)(b0 + b)].lo, all[(size_t)(b0 + b)].hi);
         int mid = sc.AddMeshData("furniture", v.data(), n.data(), (int)v.size());
         sc.AddMeshInstance(MeshInstance("furniture", mid, Mat4(), wood));
     }
