@@ -26,6 +26,10 @@ namespace
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 4;            // warps per block
 constexpr int kLd = 72;              // halves per staging row (64 + 8 pad)
+// Inference keeps the weights in shared memory with rows padded to kLd halves as well: with
+// 64-half rows the B-fragment loads of the 8 row groups of a warp all hit the same banks.
+constexpr int kWRows = 3 * 64 + kOut;
+constexpr int kWPadded = kWRows * kLd;
 
 struct WarpStage
 {
@@ -432,8 +436,8 @@ __global__ void __launch_bounds__(kWarps * 32) guide_infer_kernel(Net net, const
     if (nDev) n = *nDev;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __half* W = reinterpret_cast<__half*>(smem_raw);
-    WarpStage* stages = reinterpret_cast<WarpStage*>(smem_raw + sizeof(__half) * kWeights);
-    for (int i = threadIdx.x; i < kWeights; i += blockDim.x) W[i] = net.W[i];
+    WarpStage* stages = reinterpret_cast<WarpStage*>(smem_raw + sizeof(__half) * kWPadded);
+    for (int i = threadIdx.x; i < kWeights; i += blockDim.x) W[(i / 64) * kLd + (i % 64)] = net.W[i];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     WarpStage& ws = stages[warp];
@@ -448,14 +452,14 @@ __global__ void __launch_bounds__(kWarps * 32) guide_infer_kernel(Net net, const
         uint32_t A[4][4], H[4][4];
         float C[8][4];
         load_operand<4>(ws.x, A);
-        gemm_rows<4, 8>(A, W + kW1, 64, C);
+        gemm_rows<4, 8>(A, W + 0 * 64 * kLd, kLd, C);
         relu_operand(C, H);
-        gemm_rows<4, 8>(H, W + kW2, 64, C);
+        gemm_rows<4, 8>(H, W + 1 * 64 * kLd, kLd, C);
         relu_operand(C, A);
-        gemm_rows<4, 8>(A, W + kW3, 64, C);
+        gemm_rows<4, 8>(A, W + 2 * 64 * kLd, kLd, C);
         relu_operand(C, H);
         float Co[6][4];
-        gemm_rows<4, 6>(H, W + kW4, 64, Co);
+        gemm_rows<4, 6>(H, W + 3 * 64 * kLd, kLd, Co);
 #pragma unroll
         for (int j = 0; j < 6; ++j)
         {
@@ -509,7 +513,7 @@ __global__ void to_half_kernel(const float* a, __half* b, int n)
 }
 
 size_t train_smem() { return sizeof(SharedTrain); }
-size_t infer_smem() { return sizeof(__half) * kWeights + sizeof(WarpStage) * kWarps; }
+size_t infer_smem() { return sizeof(__half) * kWPadded + sizeof(WarpStage) * kWarps; }
 
 int launch_infer(const Net& net, const float* queries, const int* nDev, int cap, float* mix, cudaStream_t st)
 {
