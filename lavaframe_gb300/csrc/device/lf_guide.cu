@@ -30,6 +30,7 @@ constexpr int kLd = 72;              // halves per staging row (64 + 8 pad)
 // 64-half rows the B-fragment loads of the 8 row groups of a warp all hit the same banks.
 constexpr int kWRows = 3 * 64 + kOut;
 constexpr int kWPadded = kWRows * kLd;
+constexpr int kInferWarps = 8;        // warps per inference block (a lighter stage than training's)
 
 struct WarpStage
 {
@@ -38,6 +39,12 @@ struct WarpStage
     __half g[16 * kLd];              // gradients
     float out[16 * kOut];            // MLP outputs
     float dx[16 * 32];               // gradient of the grid features
+};
+
+struct InferStage
+{
+    __half x[16 * kLd];              // inputs
+    float out[16 * kOut];            // MLP outputs
 };
 
 struct SharedTrain
@@ -430,19 +437,19 @@ __global__ void guide_adam_kernel(float* master, __half* work, float* m, float* 
 
 // Mixture of every query (sample records: p, wo, n) in the compact form used for sampling:
 // per lobe mu xyz, kappa and the cumulative lobe weight.
-__global__ void __launch_bounds__(kWarps * 32) guide_infer_kernel(Net net, const float* queries, int n,
-                                                                  const int* nDev, float* mix)
+__global__ void __launch_bounds__(kInferWarps * 32) guide_infer_kernel(Net net, const float* queries, int n,
+                                                                       const int* nDev, float* mix)
 {
     if (nDev) n = *nDev;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __half* W = reinterpret_cast<__half*>(smem_raw);
-    WarpStage* stages = reinterpret_cast<WarpStage*>(smem_raw + sizeof(__half) * kWPadded);
+    InferStage* stages = reinterpret_cast<InferStage*>(smem_raw + sizeof(__half) * kWPadded);
     for (int i = threadIdx.x; i < kWeights; i += blockDim.x) W[(i / 64) * kLd + (i % 64)] = net.W[i];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    WarpStage& ws = stages[warp];
+    InferStage& ws = stages[warp];
     const int tiles = (n + 15) / 16;
-    for (int tile = blockIdx.x * kWarps + warp; tile < tiles; tile += gridDim.x * kWarps)
+    for (int tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps)
     {
         const int s = tile * 16 + (lane & 15);
         const bool valid = s < n;
@@ -513,7 +520,7 @@ __global__ void to_half_kernel(const float* a, __half* b, int n)
 }
 
 size_t train_smem() { return sizeof(SharedTrain); }
-size_t infer_smem() { return sizeof(__half) * kWPadded + sizeof(WarpStage) * kWarps; }
+size_t infer_smem() { return sizeof(__half) * kWPadded + sizeof(InferStage) * kInferWarps; }
 
 int launch_infer(const Net& net, const float* queries, const int* nDev, int cap, float* mix, cudaStream_t st)
 {
@@ -527,8 +534,9 @@ int launch_infer(const Net& net, const float* queries, const int* nDev, int cap,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tiles = (cap + 15) / 16;
-    const int blocks = std::max(1, std::min(sms * 2, (tiles + kWarps - 1) / kWarps));
-    guide_infer_kernel<<<blocks, kWarps * 32, infer_smem(), st>>>(net, queries, cap, nDev, mix);
+    const int perSm = occupancy_blocks_per_sm((const void*)guide_infer_kernel, kInferWarps * 32, infer_smem());
+    const int blocks = std::max(1, std::min(sms * perSm, (tiles + kInferWarps - 1) / kInferWarps));
+    guide_infer_kernel<<<blocks, kInferWarps * 32, infer_smem(), st>>>(net, queries, cap, nDev, mix);
     return (int)cudaGetLastError();
 }
 }
@@ -817,8 +825,8 @@ lf_status lf_guide_eval(lf_guide* gd, const float* queries, int32_t n, float* mi
         attr = true;
     }
     const int tiles = (n + 15) / 16;
-    guide_infer_kernel<<<std::max(1, std::min(4096, (tiles + kWarps - 1) / kWarps)), kWarps * 32, infer_smem(),
-                         c->stream>>>(gd->net, dq, n, nullptr, dmix);
+    guide_infer_kernel<<<std::max(1, std::min(4096, (tiles + kInferWarps - 1) / kInferWarps)), kInferWarps * 32,
+                         infer_smem(), c->stream>>>(gd->net, dq, n, nullptr, dmix);
     guide_pdf_kernel<<<grid_blocks(n, 256), 256, 0, c->stream>>>(dmix, dq, n, dpdf);
     if (mix) cudaMemcpyAsync(mix, dmix, (size_t)n * kMixFloats * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (pdf) cudaMemcpyAsync(pdf, dpdf, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
