@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
     ap.add_argument("--render-size", default="", help="c1/c3 workloads: override the resolution WxH (profiling)")
     ap.add_argument("--c4-ref-spp", type=int, default=4096, help="guiding workload reference samples")
+    ap.add_argument("--c4-alpha", type=float, default=0.5, help="guiding workload: mixture selection probability")
+    ap.add_argument("--c4-every", type=int, default=2, help="guiding workload: train after every n-th batch")
+    ap.add_argument("--c4-batch", type=int, default=16, help="guiding workload: samples per batch")
+    ap.add_argument("--c4-lr", type=float, default=1e-2, help="guiding workload: Adam learning rate")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
@@ -365,7 +369,7 @@ def run_serving(ctx, n_jobs, max_spp=256):
             "scenes": [{"generator": g, "triangles": int(sc.view().num_tris)} for g, sc in pool]}
 
 
-def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=4, every=2, max_factor=3.0):
+def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, max_factor=3.0, alpha=0.5, lr=1e-2):
     """Time-to-error of learned path guiding on the occluded-light room (16.7k boxes, ~200k
     triangles, depth 10): the plain tracer's error after plain_spp samples, against an FP64
     reference of ref_spp samples, and the wall time the guided tracer (trained online, Adam
@@ -409,7 +413,7 @@ def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=4, every=2, m
     g = lf.Guide(ctx, lo, hi, seed=1)
     f = frame()
     f.set_batch(batch)
-    f.set_guide(g, 0.5, every, 1e-2)
+    f.set_guide(g, alpha, every, lr)
     spent, done, reached, last = 0.0, 0, False, None
     while spent < max_factor * t_plain:
         t0 = time.perf_counter()
@@ -431,7 +435,7 @@ def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=4, every=2, m
             "plain_rmse": target, "guided_reached": reached, "guided_spp": done, "guided_s": spent,
             "guided_rmse": last, "time_ratio": spent / t_plain if reached else None,
             "adam_steps": st["adam_steps"], "training_samples": st["training_samples"],
-            "batch": batch, "train_every": every}
+            "batch": batch, "train_every": every, "alpha": alpha, "lr": lr}
 
 
 def main():
@@ -452,7 +456,8 @@ def main():
         ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 1024)
     if args.workload == "c4":
         cw, ch = (int(x) for x in args.c4_size.split("x"))
-        r = run_guiding(ctx, cw, ch, args.c4_ref_spp)
+        r = run_guiding(ctx, cw, ch, args.c4_ref_spp, batch=args.c4_batch, every=args.c4_every, alpha=args.c4_alpha,
+                        lr=args.c4_lr)
         if rank == 0:
             print(json.dumps({"metric": "c4 guided / plain time to the plain 1024-spp error", "value": r["time_ratio"],
                               "unit": "ratio", "higher_is_better": False, "detail": r}), flush=True)
