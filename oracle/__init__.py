@@ -30,6 +30,9 @@ def lib():
         L.lfo_math.argtypes = [C.c_int32, P, P, C.c_int64, P]
         L.lfo_rand_sequence.argtypes = [C.c_float, C.c_float, C.c_int32, C.c_uint32, C.c_int32, P]
         L.lfo_postprocess.argtypes = [P, C.c_int32, C.c_int32, P, C.c_int32, P, P]
+        L.lfo_bsdf_fn.argtypes = [C.c_int32, P, P, C.c_int64, P]
+        L.lfo_aabb.argtypes = [P, P, C.c_int64, P]
+        L.lfo_disney_samples.argtypes = [P, C.c_float, P, C.c_int32, C.c_uint32, P]
         _lib = L
     return _lib
 
@@ -43,6 +46,47 @@ def contract(fn, x, y=None):
     yy = None if y is None else np.ascontiguousarray(y, np.float32)
     out = np.empty_like(x)
     lib().lfo_math(MATH_FN[fn], x.ctypes.data, None if yy is None else yy.ctypes.data, x.size, out.ctypes.data)
+    return out
+
+
+BSDF_FN = {"dielectric_fresnel": 0, "gtr2": 1, "smith_g_ggx": 2, "gtr1": 3, "schlick_fresnel": 4}
+
+
+def bsdf_fn(fn, x, y=None):
+    """Element-wise DielectricFresnel(x, eta=y), GTR2(NdotH=x, a=y), SmithG_GGX(NdotV=x, a=y),
+    GTR1(NdotH=x, a=y) or SchlickFresnel(x) of the restated shader."""
+    x = np.ascontiguousarray(x, np.float32)
+    yy = None if y is None else np.ascontiguousarray(np.broadcast_to(y, x.shape), np.float32)
+    out = np.empty_like(x)
+    lib().lfo_bsdf_fn(BSDF_FN[fn], x.ctypes.data, None if yy is None else yy.ctypes.data, x.size, out.ctypes.data)
+    return out
+
+
+def aabb(box_min, box_max, origins, directions):
+    """AABBIntersect of each ray against one box: entry distance, exit distance from inside,
+    or -1 for a miss."""
+    box = np.ascontiguousarray(np.concatenate([box_min, box_max]), np.float32)
+    rays = np.ascontiguousarray(np.concatenate([origins, directions], axis=1), np.float32)
+    out = np.empty(len(rays), np.float32)
+    lib().lfo_aabb(box.ctypes.data, rays.ctypes.data, len(rays), out.ctypes.data)
+    return out
+
+
+MATERIAL_FIELDS = ["albedo_r", "albedo_g", "albedo_b", "specular", "emission_r", "emission_g", "emission_b",
+                   "anisotropic", "metallic", "roughness", "subsurface", "specular_tint", "sheen", "sheen_tint",
+                   "clearcoat", "clearcoat_roughness", "spec_trans", "ior", "at_distance", "extinction_r",
+                   "extinction_g", "extinction_b", "tex0", "tex1", "tex2", "tex3"]
+
+
+def disney_samples(material, eta, wo, n, seed=1):
+    """n DisneySample draws at a surface with normal +z and DisneyEval at each sampled direction:
+    an (n, 11) array of L xyz, sampled f xyz, sampled pdf, evaluated f xyz, evaluated pdf."""
+    m = np.zeros(len(MATERIAL_FIELDS), np.float32)
+    for k, v in material.items():
+        m[MATERIAL_FIELDS.index(k)] = v
+    wo = np.ascontiguousarray(wo, np.float32)
+    out = np.empty((n, 11), np.float32)
+    lib().lfo_disney_samples(m.ctypes.data, float(eta), wo.ctypes.data, n, seed, out.ctypes.data)
     return out
 
 

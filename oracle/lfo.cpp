@@ -1336,6 +1336,80 @@ int lfo_math(int32_t fn, const float* x, const float* y, int64_t n, float* out)
     return 0;
 }
 
+// Building blocks of disney.glsl / sampling.glsl / intersection.glsl for known-answer tests:
+// 0 DielectricFresnel(x, y = eta), 1 GTR2(x = NdotH, y = a), 2 SmithG_GGX(x = NdotV, y = a),
+// 3 GTR1(x = NdotH, y = a), 4 SchlickFresnel(x).
+int lfo_bsdf_fn(int32_t fn, const float* x, const float* y, int64_t n, float* out)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const float a = x[i], b = y ? y[i] : 0.f;
+        float r = 0.f;
+        switch (fn)
+        {
+        case 0: r = Shader::DielectricFresnel(a, b); break;
+        case 1: r = Shader::GTR2(a, b); break;
+        case 2: r = Shader::SmithG_GGX(a, b); break;
+        case 3: r = Shader::GTR1(a, b); break;
+        case 4: r = Shader::SchlickFresnel(a); break;
+        default: return 1;
+        }
+        out[i] = r;
+    }
+    return 0;
+}
+
+// AABBIntersect (intersection.glsl:53-68) of n rays (origin xyz, direction xyz) against one
+// box (min xyz, max xyz): the shader's return value per ray.
+int lfo_aabb(const float* box6, const float* rays6, int64_t n, float* out)
+{
+    const v3 mn(box6[0], box6[1], box6[2]), mx(box6[3], box6[4], box6[5]);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const float* r = rays6 + 6 * i;
+        float entry;
+        out[i] = AABBIntersect(mn, mx, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), &entry);
+    }
+    return 0;
+}
+
+// n DisneySample draws at a surface with normal +z (material: the 26 floats of the shader's
+// unpacked material in declaration order - albedo, specular, emission, anisotropic, metallic,
+// roughness, subsurface, specularTint, sheen, sheenTint, clearcoat, clearcoatRoughness,
+// specTrans, ior, atDistance, extinction, texture ids (ignored); refraction ratio eta; outgoing
+// direction V) with the shader's RNG seeded from `seed`; per draw: L xyz, f xyz, pdf, then
+// DisneyEval at the same L: f xyz, pdf (11 floats).
+static_assert(sizeof(Material) == 26 * sizeof(float), "unpacked material of 26 floats");
+int lfo_disney_samples(const float* mat26, float eta, const float* V3, int32_t n, uint32_t seed, float* out)
+{
+    Prepared P{};
+    Options O{0, -1.f, 0.f};
+    Counters c{};
+    Shader sh{P, O, 1, false, 0, false, false, v3(0.f), 1.f, 0.f, {seed, seed ^ 0x9E3779B9u, 7u, 11u}, c};
+    State st{};
+    std::memcpy(&st.mat, mat26, sizeof(Material));
+    for (int k = 0; k < 4; ++k) st.mat.texIDs[k] = -1.f;
+    st.eta = eta;
+    st.normal = st.ffnormal = v3(0.f, 0.f, 1.f);
+    st.tangent = v3(1.f, 0.f, 0.f);
+    st.bitangent = v3(0.f, 1.f, 0.f);
+    const v3 V(V3[0], V3[1], V3[2]);
+    for (int i = 0; i < n; ++i)
+    {
+        v3 L;
+        float pdf = 0.f, pdfE = 0.f;
+        const v3 f = sh.DisneySample(st, V, st.ffnormal, L, pdf);
+        const v3 fe = sh.DisneyEval(st, V, st.ffnormal, L, pdfE);
+        float* o = out + 11 * i;
+        o[0] = L.x; o[1] = L.y; o[2] = L.z;
+        o[3] = f.x; o[4] = f.y; o[5] = f.z;
+        o[6] = pdf;
+        o[7] = fe.x; o[8] = fe.y; o[9] = fe.z;
+        o[10] = pdfE;
+    }
+    return 0;
+}
+
 // PCG4D random sequence of the shader (globals.glsl:116-133) for one pixel/frame.
 int lfo_rand_sequence(float px, float py, int32_t frame, uint32_t seed_fold, int32_t n, float* out)
 {
