@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
+    ap.add_argument("--host-chunks", type=int, default=0,
+                    help="pieces of the host-buffer pass whose copies overlap tracing (0 = the library's choice)")
     ap.add_argument("--spp-batch", type=int, default=0, help="samples per wavefront batch of the render workloads")
     ap.add_argument("--frame-flags", type=int, default=0, help="lf_frame flags of the render workloads (8 = per-batch)")
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
@@ -514,6 +516,7 @@ def main():
     ctx._c(L.lf_host_alloc(ctx.h, nrays * 16, C.byref(h_hits)))
     C.memmove(h_rays, rays.ctypes.data, rays.nbytes)
     fr = C.cast(h_rays, C.POINTER(C.c_float))
+    ctx.set_host_chunks(args.host_chunks)
     for _ in range(args.warmup if e2e_steps else 1):
         ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, nrays, h_hits, 0))
     barrier(world)

@@ -203,10 +203,17 @@ typedef struct lf_hit
 #define LF_TRACE_UNSORTED 0x4 /* trace in input order (no binning by origin cell and octant) */
 #define LF_TRACE_SIMPLE 0x8   /* one thread per ray, no persistent warps */
 
-/* Host buffers: copies rays in, traces, copies hits out (synchronous). */
+/* Host buffers: copies rays in, traces, copies hits out (synchronous). When the output lies
+ * in one block from lf_host_alloc of this context, the kernels write the results there and
+ * nothing is copied back. */
 lf_status lf_trace_closest(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, lf_hit* hits, uint32_t flags);
 /* occluded[i] = 1 when something lies closer than tmax. */
 lf_status lf_trace_any(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, uint8_t* occluded, uint32_t flags);
+/* Host-buffer queries split the rays into `chunks` pieces (1..8; 0 = automatic, the
+ * default: two pieces from 2^24 rays up, else one): piece k+1 is copied in and piece k-1
+ * copied out while piece k is sorted and traced. Every ray's result is the same for any
+ * setting; LF_TRACE_STATS queries run whole. */
+lf_status lf_ctx_set_host_chunks(lf_ctx* c, int32_t chunks);
 /* Device buffers, asynchronous on the context stream (lf_ctx_sync to wait). */
 lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_hits,
                                   uint32_t flags);
@@ -216,7 +223,8 @@ lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64
  * leaf visits (sums over all rays). */
 lf_status lf_trace_stats(const lf_ctx* c, uint64_t out3[3]);
 
-/* Page-locked host memory (fast host<->device copies), e.g. for ray and hit buffers. */
+/* Page-locked host memory, mapped into the device's address space (fast host<->device
+ * copies; host queries write their results straight into it), e.g. for ray and hit buffers. */
 lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out);
 lf_status lf_host_free(lf_ctx* c, void* p);
 /* Device memory helpers for callers without their own allocator. */

@@ -65,6 +65,7 @@ _SIG = {
     "lf_ctx_timer_start": (C.c_int, [_P]),
     "lf_ctx_timer_stop": (C.c_int, [_P, _F]),
     "lf_ctx_configure_engine": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "lf_ctx_set_host_chunks": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_engine_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "lf_scene_upload": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_scene_update_instances": (C.c_int, [_P, _P]),
@@ -367,6 +368,10 @@ class Context:
         (0 = keep the pool / default)."""
         self._c(lib().lf_ctx_configure_engine(self.h, slots, block_extend, block_shade, block_shadow,
                                               shade_threads_per_sm))
+
+    def set_host_chunks(self, chunks=0):
+        """Pieces of host-buffer ray queries whose copies overlap tracing (0 = automatic)."""
+        self._c(lib().lf_ctx_set_host_chunks(self.h, chunks))
 
     def engine_info(self):
         slots, nbytes = C.c_int64(), C.c_int64()

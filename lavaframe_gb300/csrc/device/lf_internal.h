@@ -38,6 +38,21 @@ struct lf_ctx
     void* scratchOut = nullptr;
     size_t scratchOutBytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // pieces of the host-pointer ray queries: copy streams and one event per piece and side
+    static constexpr int kMaxHostChunks = 8;
+    int hostChunks = 0;                       // 0: automatic
+    cudaStream_t copyIn = nullptr, copyOut = nullptr;
+    cudaEvent_t chunkIn[kMaxHostChunks] = {}, chunkDone[kMaxHostChunks] = {};
+    cudaEvent_t chunkStart = nullptr, chunkEnd = nullptr;
+    // page-locked blocks from lf_host_alloc and their device addresses: results of host queries
+    // whose output lies in one are written there by the kernels, without a copy back
+    struct HostBlock
+    {
+        char* host;
+        char* dev;
+        size_t bytes;
+    };
+    std::vector<HostBlock> hostBlocks;
     // scratch of the binned ray queries
     uint32_t* binKeys = nullptr;
     int* binPerm = nullptr;

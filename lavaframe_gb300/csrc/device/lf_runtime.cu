@@ -57,6 +57,15 @@ void lf_ctx_destroy(lf_ctx* c)
     cudaFree(c->binNext);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (int k = 0; k < lf_ctx::kMaxHostChunks; ++k)
+    {
+        if (c->chunkIn[k]) cudaEventDestroy(c->chunkIn[k]);
+        if (c->chunkDone[k]) cudaEventDestroy(c->chunkDone[k]);
+    }
+    if (c->chunkStart) cudaEventDestroy(c->chunkStart);
+    if (c->chunkEnd) cudaEventDestroy(c->chunkEnd);
+    if (c->copyIn) cudaStreamDestroy(c->copyIn);
+    if (c->copyOut) cudaStreamDestroy(c->copyOut);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -97,15 +106,32 @@ lf_status lf_ctx_timer_stop(lf_ctx* c, float* ms)
 lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out)
 {
     if (!c || !out) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
     cudaSetDevice(c->device);
-    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
-    return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaMallocHost");
+    const size_t size = bytes ? bytes : 1;
+    cudaError_t e = cudaHostAlloc(out, size, cudaHostAllocMapped);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaHostAlloc");
+    void* dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, *out, 0) != cudaSuccess)
+    {
+        cudaGetLastError();
+        dev = nullptr;   // not reachable from kernels: host queries copy their results back
+    }
+    c->hostBlocks.push_back({(char*)*out, (char*)dev, size});
+    return LF_OK;
 }
 
 lf_status lf_host_free(lf_ctx* c, void* p)
 {
     if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
     cudaSetDevice(c->device);
+    for (size_t i = 0; i < c->hostBlocks.size(); ++i)
+        if (c->hostBlocks[i].host == (char*)p)
+        {
+            c->hostBlocks.erase(c->hostBlocks.begin() + (long)i);
+            break;
+        }
     cudaError_t e = cudaFreeHost(p);
     return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "cudaFreeHost");
 }
@@ -893,6 +919,50 @@ lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64
 
 namespace
 {
+// Pieces of a host-buffer query: the setting, else two from 2^24 rays up and one below. A
+// piece is sorted and traced on its own, so its bins are sparser: on 10.5M triangles a piece
+// of 2^23 rays traces 2 % slower than 2^24 rays at once and one of 2^22 rays 5 % slower;
+// two pieces hide half of the copy in and gain 1-2 %, four lose.
+int host_chunks(const lf_ctx* c, int64_t n, uint32_t flags)
+{
+    if (flags & LF_TRACE_STATS) return 1;
+    int k = c->hostChunks > 0 ? c->hostChunks : (n >= (int64_t(1) << 24) ? 2 : 1);
+    k = std::max(1, std::min(k, lf_ctx::kMaxHostChunks));
+    return n >= 1024 * (int64_t)k ? k : 1;
+}
+
+cudaError_t ensure_chunk_streams(lf_ctx* c)
+{
+    if (c->copyOut) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copyIn, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copyOut, cudaStreamNonBlocking);
+    for (int k = 0; k < lf_ctx::kMaxHostChunks && e == cudaSuccess; ++k)
+    {
+        e = cudaEventCreateWithFlags(&c->chunkIn[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->chunkDone[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->chunkStart, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->chunkEnd, cudaEventDisableTiming);
+    return e;
+}
+
+// Device address of [p, p + bytes) when the whole range lies in one page-locked block that
+// lf_host_alloc of this context made and mapped, else null.
+char* mapped_range(const lf_ctx* c, const void* p, size_t bytes)
+{
+    const char* q = (const char*)p;
+    for (const auto& h : c->hostBlocks)
+        if (h.dev && q >= h.host && bytes <= h.bytes && (size_t)(q - h.host) <= h.bytes - bytes)
+            return h.dev + (q - h.host);
+    return nullptr;
+}
+
+// Copies the rays in, traces them and copies the results out, in `host_chunks` pieces: piece k
+// is copied in on copyIn, sorted and traced on the context stream once its copy is done, and
+// copied out on copyOut once traced, so copies of some pieces overlap the tracing of others.
+// When the results go to a mapped page-locked block of this context, the kernels write them
+// there and nothing is copied out. The context stream waits for the copy streams, and the
+// call returns after it.
 template <class Launch>
 lf_status trace_host(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, void* out, size_t outElem, uint32_t flags,
                      Launch launch)
@@ -911,14 +981,53 @@ lf_status trace_host(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, void
         if (err == cudaSuccess) *cap = bytes;
         return err;
     };
+    char* direct = mapped_range(c, out, (size_t)n * outElem);
     cudaError_t e = ensure(&c->scratchRays, &c->scratchRaysBytes, (size_t)n * 32);
-    if (e == cudaSuccess) e = ensure(&c->scratchOut, &c->scratchOutBytes, (size_t)n * outElem);
-    void* d_rays = c->scratchRays;
-    void* d_out = c->scratchOut;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && !direct) e = ensure(&c->scratchOut, &c->scratchOutBytes, (size_t)n * outElem);
+    const int K = host_chunks(c, n, flags);
+    if (e == cudaSuccess && K > 1) e = ensure_chunk_streams(c);
+    char* d_rays = (char*)c->scratchRays;
+    char* d_out = direct ? direct : (char*)c->scratchOut;
     lf_status st = LF_OK;
-    if (e == cudaSuccess) st = launch(d_rays, d_out);
-    if (e == cudaSuccess && st == LF_OK) e = cudaMemcpyAsync(out, d_out, (size_t)n * outElem, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && K == 1)
+    {
+        e = cudaMemcpyAsync(d_rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) st = launch(d_rays, d_out, n);
+        if (e == cudaSuccess && st == LF_OK && !direct)
+            e = cudaMemcpyAsync(out, d_out, (size_t)n * outElem, cudaMemcpyDeviceToHost, c->stream);
+    }
+    else if (e == cudaSuccess)
+    {
+        // pieces of whole 1024-ray groups; the last takes the rest
+        const int64_t step = ((n / K) + 1023) / 1024 * 1024;
+        e = cudaEventRecord(c->chunkStart, c->stream);   // after earlier users of the scratch
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copyIn, c->chunkStart, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copyOut, c->chunkStart, 0);
+        for (int k = 0; k < K && e == cudaSuccess; ++k)
+        {
+            const int64_t lo = std::min(n, step * k), hi = k == K - 1 ? n : std::min(n, step * (k + 1));
+            e = cudaMemcpyAsync(d_rays + lo * 32, (const char*)rays + lo * 32, (size_t)(hi - lo) * 32,
+                                cudaMemcpyHostToDevice, c->copyIn);
+            if (e == cudaSuccess) e = cudaEventRecord(c->chunkIn[k], c->copyIn);
+        }
+        for (int k = 0; k < K && e == cudaSuccess && st == LF_OK; ++k)
+        {
+            const int64_t lo = std::min(n, step * k), hi = k == K - 1 ? n : std::min(n, step * (k + 1));
+            e = cudaStreamWaitEvent(c->stream, c->chunkIn[k], 0);
+            if (e == cudaSuccess && hi > lo) st = launch(d_rays + lo * 32, d_out + lo * outElem, hi - lo);
+            if (direct) continue;
+            if (e == cudaSuccess && st == LF_OK) e = cudaEventRecord(c->chunkDone[k], c->stream);
+            if (e == cudaSuccess && st == LF_OK) e = cudaStreamWaitEvent(c->copyOut, c->chunkDone[k], 0);
+            if (e == cudaSuccess && st == LF_OK)
+                e = cudaMemcpyAsync((char*)out + lo * outElem, d_out + lo * outElem, (size_t)(hi - lo) * outElem,
+                                    cudaMemcpyDeviceToHost, c->copyOut);
+        }
+        // the context stream waits for both copy streams whatever happened above
+        cudaEventRecord(c->chunkEnd, c->copyIn);
+        cudaStreamWaitEvent(c->stream, c->chunkEnd, 0);
+        cudaEventRecord(c->chunkEnd, c->copyOut);
+        cudaStreamWaitEvent(c->stream, c->chunkEnd, 0);
+    }
     if (e == cudaSuccess && st == LF_OK) st = check_device(c);
     if (e == cudaSuccess && st == LF_OK && (flags & LF_TRACE_STATS))
     {
@@ -933,17 +1042,25 @@ lf_status trace_host(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, void
 
 extern "C" {
 
+lf_status lf_ctx_set_host_chunks(lf_ctx* c, int32_t chunks)
+{
+    if (!c || chunks < 0 || chunks > lf_ctx::kMaxHostChunks) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    c->hostChunks = chunks;
+    return LF_OK;
+}
+
 lf_status lf_trace_closest(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, lf_hit* hits, uint32_t flags)
 {
-    return trace_host(c, sc, rays, n, hits, sizeof(lf_hit), flags, [&](void* dr, void* dout) {
-        return lf_trace_closest_device(c, sc, dr, n, dout, flags);
+    return trace_host(c, sc, rays, n, hits, sizeof(lf_hit), flags, [&](void* dr, void* dout, int64_t m) {
+        return lf_trace_closest_device(c, sc, dr, m, dout, flags);
     });
 }
 
 lf_status lf_trace_any(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, uint8_t* occ, uint32_t flags)
 {
-    return trace_host(c, sc, rays, n, occ, 1, flags, [&](void* dr, void* dout) {
-        return lf_trace_any_device(c, sc, dr, n, dout, flags);
+    return trace_host(c, sc, rays, n, occ, 1, flags, [&](void* dr, void* dout, int64_t m) {
+        return lf_trace_any_device(c, sc, dr, m, dout, flags);
     });
 }
 

@@ -2,7 +2,8 @@
 start outside the scene or point away from it, zero-length and negative segments, frames of
 one pixel and ragged tiles, and the full 10.5M-triangle microbench scene checked through
 size-independent properties (any-hit answers the closest-hit question exactly; an oracle spot
-check; every hit lies within the segment)."""
+check; every hit lies within the segment), and host queries split into pieces whose copies
+overlap tracing."""
 import numpy as np
 import pytest
 
@@ -31,6 +32,60 @@ def test_empty_and_ragged_batches(ctx, n):
         assert compare_hits(hits, ref) == 0
         ref_occ, _ = oracle.trace_any(s.view(), rays)
         assert np.array_equal(occ, ref_occ)
+    ds.close()
+
+
+@pytest.mark.parametrize("chunks", [2, 3, 8])
+def test_host_queries_in_pieces_match_whole(ctx, chunks):
+    # pieces are sorted and traced on their own while the others are copied; every ray's
+    # answer must be the one of the whole query (ragged sizes: the last piece takes the rest)
+    s = small_soup()
+    ds = ctx.upload(s)
+    for n in (1, 1023, 3 * 4097 + 5):
+        rays = soup_rays(s, n, seed=13)
+        ctx.set_host_chunks(1)
+        whole, whole_occ = ctx.trace_closest(ds, rays), ctx.trace_any(ds, rays)
+        ctx.set_host_chunks(chunks)
+        try:
+            hits, occ = ctx.trace_closest(ds, rays), ctx.trace_any(ds, rays)
+        finally:
+            ctx.set_host_chunks(0)
+        assert hits.tobytes() == whole.tobytes() and np.array_equal(occ, whole_occ)
+        ref, _ = oracle.trace_closest(s.view(), rays)
+        assert compare_hits(hits, ref) == 0
+    ds.close()
+
+
+def test_results_written_into_mapped_host_blocks(ctx):
+    # an output range inside a block from lf_host_alloc is written by the kernels directly
+    # (whole query or pieces); the answers equal those copied back into pageable memory
+    import ctypes as C
+
+    s = small_soup()
+    ds = ctx.upload(s)
+    n = 3 * 4097 + 5
+    rays = soup_rays(s, n, seed=14)
+    whole = ctx.trace_closest(ds, rays)
+    whole_occ = ctx.trace_any(ds, rays)
+    L = lf.lib()
+    size = n * 16 + 64
+    blk = C.c_void_p()
+    ctx._c(L.lf_host_alloc(ctx.h, size, C.byref(blk)))
+    fr = rays.ctypes.data_as(C.POINTER(C.c_float))
+    try:
+        for chunks in (1, 3):
+            ctx.set_host_chunks(chunks)
+            for off in (0, 48):
+                C.memset(blk.value, 0xFF, size)
+                ctx._c(L.lf_trace_closest(ctx.h, ds.h, fr, n, blk.value + off, 0))
+                assert bytes((C.c_char * (n * 16)).from_address(blk.value + off)) == whole.tobytes()
+            C.memset(blk.value, 0xFF, size)
+            ctx._c(L.lf_trace_any(ctx.h, ds.h, fr, n, blk.value + 5, 0))
+            got = np.frombuffer(bytes((C.c_char * n).from_address(blk.value + 5)), np.uint8)
+            assert np.array_equal(got, whole_occ)
+    finally:
+        ctx.set_host_chunks(0)
+        ctx._c(L.lf_host_free(ctx.h, blk))
     ds.close()
 
 
@@ -106,4 +161,10 @@ def test_full_microbench_scene_properties(ctx):
     idx = np.random.default_rng(5).choice(len(rays), 2048, replace=False)
     ref, _ = oracle.trace_closest(s.view(), rays[idx])
     assert compare_hits(hits[idx], ref) == 0
+    # the same query in four pieces, with copies overlapping the tracing
+    ctx.set_host_chunks(4)
+    try:
+        assert ctx.trace_closest(ds, rays).tobytes() == hits.tobytes()
+    finally:
+        ctx.set_host_chunks(0)
     ds.close()
