@@ -61,7 +61,7 @@ struct EngineCtl
 
 struct EngineBuffers
 {
-    PathSoA ps;                  // info: x local path id, y depth, z last material, w ring | job << 14
+    PathSoA ps;                  // info: x radiance entry in the pass, y depth, z last material, w ring | job << 14
     int* queue[2];
     ShadowRec* shadow;
     int* done[2];                // slots whose path finished
