@@ -21,6 +21,8 @@ using namespace pathops;
 
 
 // ------------------------------------------------------------------ generate
+// Slot s * tilePix + lp starts sample s of tile pixel pixel_of(lp) (8 x 4 blocks), so a
+// warp's camera rays cover a compact patch; info.x holds the pixel for the accumulation.
 __global__ void generate_kernel(ShadeScene S, Params P, PathSoA ps, int firstSample, int nSamples, int* queue,
                                 int* qcount)
 {
@@ -38,7 +40,8 @@ __global__ void generate_kernel(ShadeScene S, Params P, PathSoA ps, int firstSam
         {
             int s = (int)(i / tilePix);
             int lp = (int)(i - (long long)s * tilePix);
-            int lx = lp % P.tileW, ly = lp / P.tileW;
+            int lx, ly;
+            pixel_of(lp, P.tileW, P.tileH, lx, ly);   // the same pixel for every sample of lp
             int gx = P.tileX * P.tileW + lx, gy = P.tileY * P.tileH + ly;
             bool inside = gx < P.width && gy < P.height;
             ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);

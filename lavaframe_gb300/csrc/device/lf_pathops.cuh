@@ -5,6 +5,7 @@
 
 #include "lf_guide.cuh"
 #include "lf_kernels.h"
+#include "lf_pixel.h"
 
 namespace lfd
 {

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "lf_engine_host.h"
+#include "lf_pixel.h"
 
 using namespace lfrt;
 
@@ -1517,17 +1518,33 @@ lf_status lf_frame_read_paths(lf_frame* f, float* rgb, int32_t max_samples)
     const float4* src = f->lastRadiance ? f->lastRadiance : f->ps.L;
     int n = std::min(max_samples, f->lastRadiance ? f->lastRadianceSamples : f->lastBatchSamples);
     if (!src || n <= 0) return fail(c, LF_ERR_STATE, "no rendered paths to read");
-    size_t pix = (size_t)f->W * f->H;
-    std::vector<float4> tmp(pix * n);
+    const size_t pix = (size_t)f->W * f->H;
+    // the engine's pass buffer is [sample][pixel]; the per-batch slots are [sample][tile
+    // position] with the tile's pixels in pixel_of order
+    const bool slots = !f->lastRadiance;
+    const int tw = f->P.tileW, th = f->P.tileH;
+    const size_t per = slots ? (size_t)tw * th : pix;
+    std::vector<float4> tmp(per * n);
     cudaError_t e = cudaMemcpyAsync(tmp.data(), src, tmp.size() * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "path readback");
-    for (size_t i = 0; i < tmp.size(); ++i)
-    {
-        rgb[i * 3 + 0] = tmp[i].x;
-        rgb[i * 3 + 1] = tmp[i].y;
-        rgb[i * 3 + 2] = tmp[i].z;
-    }
+    for (int s = 0; s < n; ++s)
+        for (size_t k = 0; k < per; ++k)
+        {
+            size_t i = k;
+            if (slots)
+            {
+                int x, y;
+                pixel_of((int)k, tw, th, x, y);
+                if (x >= f->W || y >= f->H) continue;
+                i = (size_t)y * f->W + x;
+            }
+            const float4 v = tmp[(size_t)s * per + k];
+            float* d = rgb + ((size_t)s * pix + i) * 3;
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+        }
     return check_device(c);
 }
 
