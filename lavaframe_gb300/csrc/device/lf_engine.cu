@@ -121,6 +121,8 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
     c->shadeNext = 0;
     c->shadowNext = 0;
     c->refillNext = 0;
+    c->hitCount = 0;
+    c->missCount = 0;
 }
 
 // ------------------------------------------------------------------ finish / refill
@@ -250,22 +252,41 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const int i = base + lane;
-        if (i >= n) continue;
-        const int p = q[i];
-        const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
-        Hit h;
-        uint32_t err;
-        if constexpr (kOne)
-            err = closest_hit<false>(one.S.trav, f3(o4), f3(d4), kInfinity, one.P.useLights != 0, &h, nullptr);
-        else
+        int p = -1;
+        bool miss = false;
+        if (i < n)
         {
-            const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
-            const EngineJob& J = b.jobs[job_of(w)];
-            const DevScene T = J.S.trav;
-            err = closest_hit<false>(T, f3(o4), f3(d4), kInfinity, J.P.useLights != 0, &h, nullptr);
+            p = q[i];
+            const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
+            Hit h;
+            uint32_t err;
+            if constexpr (kOne)
+                err = closest_hit<false>(one.S.trav, f3(o4), f3(d4), kInfinity, one.P.useLights != 0, &h, nullptr);
+            else
+            {
+                const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
+                const EngineJob& J = b.jobs[job_of(w)];
+                const DevScene T = J.S.trav;
+                err = closest_hit<false>(T, f3(o4), f3(d4), kInfinity, J.P.useLights != 0, &h, nullptr);
+            }
+            b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
+            set_error(b.status, err);
+            miss = h.t == kInfinity;   // the shade kernel's environment case
         }
-        b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
-        set_error(b.status, err);
+        // hits count up from the front of `part`, misses down from the back; together they
+        // are the n queued paths, so the two ranges never meet
+        const unsigned hm = __ballot_sync(kFull, p >= 0 && !miss), mm = __ballot_sync(kFull, p >= 0 && miss);
+        int hb = 0, mb = 0;
+        if (lane == 0)
+        {
+            if (hm) hb = atomicAdd(&b.ctl->hitCount, __popc(hm));
+            if (mm) mb = atomicAdd(&b.ctl->missCount, __popc(mm));
+        }
+        hb = __shfl_sync(kFull, hb, 0);
+        mb = __shfl_sync(kFull, mb, 0);
+        const unsigned below = (1u << lane) - 1u;
+        if (p >= 0 && !miss) b.part[hb + __popc(hm & below)] = p;
+        if (p >= 0 && miss) b.part[b.cap - 1 - (mb + __popc(mm & below))] = p;
     }
 }
 
@@ -279,7 +300,7 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
 {
     EngineCtl* ctl = b.ctl;
     const int n = ctl->count[parity];
-    const int* qin = b.queue[parity];
+    const int nHit = ctl->hitCount;   // part: hits at [0, nHit), misses at the back
     int* qout = b.queue[parity ^ 1];
     const int lane = threadIdx.x & 31;
     while (true)
@@ -296,7 +317,7 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
         ShadowRec rec;
         if (i < n)
         {
-            p = qin[i];
+            p = i < nHit ? b.part[i] : b.part[b.cap - 1 - (i - nHit)];
             if constexpr (kOne)
                 shade_path<kLights>(one.S, one.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
             else

@@ -13,8 +13,9 @@
 //   finish   done[k]: write out finished paths, count pass completions, free their slots
 //   refill   start new paths in free slots while unissued ids remain (-> queue[k])
 //   reset    commit the refill, clear done[k], the shadow queue and queue[k^1]
-//   extend   closest hit of every queued path
-//   shade    one PathTrace bounce; survivors -> queue[k^1], finished -> done[k^1]
+//   extend   closest hit of every queued path; hits and misses -> part (front and back)
+//   shade    one PathTrace bounce over part's hits, then its misses, so that a warp shades
+//            one kind; survivors -> queue[k^1], finished -> done[k^1]
 //   shadow   next-event visibility
 #pragma once
 
@@ -57,12 +58,14 @@ struct EngineCtl
     int taken;                     // slots the current step's refill started
     int extendNext, shadeNext, shadowNext;   // work counters of the extend, shade and shadow kernels
     int refillNext;                // ids handed out by the current refill
+    int hitCount, missCount;       // the extension queue split by extend: hits, then misses
 };
 
 struct EngineBuffers
 {
     PathSoA ps;                  // info: x radiance entry in the pass, y depth, z last material, w ring | job << 14
     int* queue[2];
+    int* part;                   // extended paths: hits from the front, misses from the back
     ShadowRec* shadow;
     int* done[2];                // slots whose path finished
     EngineCtl* ctl;

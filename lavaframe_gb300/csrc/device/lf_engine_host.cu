@@ -50,6 +50,7 @@ lf_status alloc_pool(EngineHost* e, int slots)
     A(&b.ps.hit, slots);
     A(&b.queue[0], slots);
     A(&b.queue[1], slots);
+    A(&b.part, slots);
     A(&b.done[0], slots);
     A(&b.done[1], slots);
     A(&b.shadow, slots);
