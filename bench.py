@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--spp-batch", type=int, default=0, help="samples per wavefront batch of the render workloads")
     ap.add_argument("--frame-flags", type=int, default=0, help="lf_frame flags of the render workloads (8 = per-batch)")
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
-    ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768/1024; 0 = 1024)")
+    ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768/1024; 0 = 512)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
@@ -455,7 +455,7 @@ def main():
     b.build_oracle()
     ctx = lf.Context(local)
     if args.engine_slots or args.shade_cap:
-        ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 1024)
+        ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 512)
     if args.workload == "c4":
         cw, ch = (int(x) for x in args.c4_size.split("x"))
         r = run_guiding(ctx, cw, ch, args.c4_ref_spp, batch=args.c4_batch, every=args.c4_every, alpha=args.c4_alpha,

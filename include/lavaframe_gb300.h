@@ -277,7 +277,7 @@ lf_status lf_frame_release(lf_frame* f);
  * GL draw). `slots` = path slots in the pool (0 keeps the current pool), block sizes of the
  * extend / shade / shadow kernels (0 = default 128; multiples of 32 up to 1024, shade up to
  * 256), and the register cap of the shade kernel as the threads per SM it must fit (0 = none,
- * 512, 768 or 1024). The engine starts with 2^24 slots and a cap of 1024. Fails with LF_ERR_STATE
+ * 512, 768 or 1024). The engine starts with 2^24 slots and a cap of 512. Fails with LF_ERR_STATE
  * while passes are in flight. */
 lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend, int32_t block_shade,
                                   int32_t block_shadow, int32_t shade_threads_per_sm);

@@ -17,7 +17,7 @@ CANDIDATES = {
     "block_extend": [64, 128, 256],
     "block_shadow": [64, 128, 256],
 }
-DEFAULT = {"slots": 1 << 24, "shade_threads_per_sm": 1024, "block_extend": 128, "block_shadow": 128}
+DEFAULT = {"slots": 1 << 24, "shade_threads_per_sm": 512, "block_extend": 128, "block_shadow": 128}
 MARGIN = 0.02   # a setting replaces the current one only when it is this much faster (timing noise)
 
 

@@ -514,7 +514,10 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
     const int bw = b.blockShadow > 0 ? b.blockShadow : 128;
     engine_extend_kernel<kOne><<<full_grid((const void*)engine_extend_kernel<kOne>, be, b.cap), be, 0, st>>>(b, one,
                                                                                                            parity);
-    if (b.shadeThreadsPerSm == 512)
+    if (b.shadeThreadsPerSm == 512 && kOne && !one.P.useLights)
+        engine_shade_kernel<kOne, 512, false><<<full_grid((const void*)engine_shade_kernel<kOne, 512, false>, bs, b.cap),
+                                                bs, 0, st>>>(b, one, parity);
+    else if (b.shadeThreadsPerSm == 512)
         engine_shade_kernel<kOne, 512><<<full_grid((const void*)engine_shade_kernel<kOne, 512>, bs, b.cap), bs, 0, st>>>(
             b, one, parity);
     else if (b.shadeThreadsPerSm == 768)

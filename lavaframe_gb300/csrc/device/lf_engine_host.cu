@@ -12,7 +12,7 @@ namespace lfrt
 namespace
 {
 constexpr int kDefaultSlots = 1 << 24;      // ~4.6 GB of path state (2^23 measured 2-3 % slower on C3)
-constexpr int kDefaultShadeCap = 1024;      // shade kernel register cap (threads per SM)
+constexpr int kDefaultShadeCap = 512;       // shade kernel register cap (threads per SM)
 constexpr int kMaxJobs = 4096;
 constexpr size_t kRunRadianceBytes = size_t(2) << 30;   // radiance buffers of one frame run
 

@@ -14,7 +14,7 @@ from tests import scenes
 pytestmark = pytest.mark.gpu
 
 DEFAULT_SLOTS = 1 << 24
-DEFAULT_SHADE_CAP = 1024
+DEFAULT_SHADE_CAP = 512
 
 
 def icospheres():
