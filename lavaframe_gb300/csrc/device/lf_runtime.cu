@@ -1030,6 +1030,7 @@ lf_status trace_host(lf_ctx* c, lf_scene* sc, const float* rays, int64_t n, void
         cudaStreamWaitEvent(c->stream, c->chunkEnd, 0);
     }
     if (e == cudaSuccess && st == LF_OK) st = check_device(c);
+    else cudaStreamSynchronize(c->stream);   // no copy may still touch the caller's buffers
     if (e == cudaSuccess && st == LF_OK && (flags & LF_TRACE_STATS))
     {
         unsigned long long s[3];
