@@ -13,7 +13,7 @@
 //    accumulation by it, like postprocess.glsl's invSampleCounter;
 //  - a moved camera or edited instances reset the accumulation (TiledRenderer.cpp:471-484).
 // There is no GL: Present/SetViewport are no-ops returning 0, Denoise is not available
-// (the reference's OIDN binary is not part of this build) and returns 0.
+// (the reference's OIDN binary is not part of this library) and returns 0.
 #pragma once
 
 #include <cmath>

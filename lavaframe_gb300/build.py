@@ -1,13 +1,13 @@
 """Builds the native libraries in-tree.
 
   lavaframe_gb300/liblfcore.so   product: host scene layer + CUDA kernels (sm_103a) + C ABI
-  oracle/liblfo.so               CPU checker (test infrastructure only)
+  oracle/liblfo.so               CPU oracle (test infrastructure only)
   oracle/_ref/*                  reference code compiled from a local reference checkout
                                  (only when one is available; never shipped)
 
 Host C++ is compiled with -ffp-contract=off and device code with --fmad=false: the BVH
 build and the path-tracing arithmetic must not be contracted into fused multiply-adds,
-otherwise results stop being bit-identical between the host checker and the GPU.
+otherwise results stop being bit-identical between the CPU oracle and the GPU.
 """
 from __future__ import annotations
 

@@ -104,7 +104,7 @@ lf_status engine_get(lf_ctx* c, EngineHost** out)
     e->jobUsed.assign(kMaxJobs, 0);
     e->jobGen.assign(kMaxJobs, 0);
     // pass radiance buffers come from the stream-ordered pool; keep up to 8 GB of it cached
-    // between runs instead of returning it to the driver at every synchronisation
+    // between runs instead of handing it back to CUDA at every synchronisation
     cudaMemPool_t pool = nullptr;
     if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess)
     {

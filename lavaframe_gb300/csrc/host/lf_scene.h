@@ -10,7 +10,7 @@
 //   HDRData/HDRLoader LavaFrame/hdrloader.h:19-33, hdrloader.cpp:57-204
 //   Scene             LavaFrame/Scene.h:47-107, Scene.cpp
 // Additions (no reference counterpart): in-memory mesh and environment input
-// (AddMeshData, AddHDRData), the spec aliases AddEnvMap/ProcessScene, and
+// (AddMeshData, AddHDRData), the aliases AddEnvMap/ProcessScene, and
 // ValidateForDevice. Errors are reported through return values and LastError(), never by
 // aborting.
 #pragma once

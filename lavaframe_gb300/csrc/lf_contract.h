@@ -1,5 +1,5 @@
 // Arithmetic contract of the path tracer: one definition of every operation whose result
-// GLSL leaves to the implementation, shared by the CUDA kernels and the CPU checker.
+// GLSL leaves to the implementation, shared by the CUDA kernels and the CPU oracle.
 //
 // GLSL 3.30 fixes the formulas of min/max/clamp/mix/reflect/refract/dot/cross but not the
 // precision of sin/cos/tan/acos/atan/exp/log/pow, nor how `inverse()` or texture filtering

@@ -2,7 +2,7 @@
 // Formulas are the ones the GLSL specification states (dot, cross, normalize = x/length,
 // reflect, refract, mix, clamp, min, max), evaluated left to right in IEEE single
 // precision; transcendental functions come from lf_contract.h. Shared by the CUDA kernels
-// and the CPU checker so that both run the same operation sequence.
+// and the CPU oracle so that both run the same operation sequence.
 #pragma once
 
 #include "lf_contract.h"

@@ -1,7 +1,7 @@
 """CPU oracle (test infrastructure): ctypes wrapper of oracle/liblfo.so.
 
 The oracle restates the reference GLSL path tracer in scalar C++ and runs it on the host
-cores. Only tests, the smoke check and the bench's CPU-baseline leg use it, as the checker;
+cores. Only tests, the smoke check and the bench's CPU-baseline leg use it, to check results;
 the product path never imports it.
 """
 from __future__ import annotations

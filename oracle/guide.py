@@ -18,7 +18,7 @@ The model (identical definition to the device kernels in lavaframe_gb300/csrc/de
                 objective of neural importance sampling, Mueller et al. 2019).
 
 No reference counterpart: LavaFrame samples directions from the BSDF only. Only tests use this
-module, as the checker of the device gradients.
+module, to check the device gradients.
 """
 from __future__ import annotations
 

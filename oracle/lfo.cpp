@@ -1,7 +1,7 @@
 // Oracle: scalar C++ restatement of the reference path tracer (shaders/renderer.glsl and
 // shaders/common/{globals,intersection,closest_hit,anyhit,sampling,disney,pathtrace}.glsl),
 // run multithreaded on the host. TEST INFRASTRUCTURE ONLY: tests, the smoke check and the
-// bench's CPU baseline load it as the checker; the product never links or calls it.
+// bench's CPU baseline load it to check results; the product never links or calls it.
 //
 // It reads the scene in the reference's own flat layouts (36-byte nodes with float-encoded
 // indices, int3 triangle indices, float4 vertices/normals, 112-byte materials, 64-byte
