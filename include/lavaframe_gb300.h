@@ -301,12 +301,19 @@ typedef struct lf_post_params
 /* rgb8 (W*H*3 bytes) and/or rgbf (W*H*3 floats, after tone map and vignette, before the
  * 8-bit conversion); row 0 = bottom as in GL. `samples` = the accumulated sample count. */
 lf_status lf_frame_postprocess(lf_frame* f, const lf_post_params* p, int32_t samples, uint8_t* rgb8, float* rgbf);
-/* Image export (Export.h:14-151 writes through stb/tinyexr; here): PNG (8-bit RGB), PPM (8-bit
- * RGB) and PFM (float RGB). Input rows are bottom-first as the frame buffers; PNG and PPM are
- * written top row first (the reference flips on write), PFM bottom-first as the format wants. */
+/* Image export (Export.h:14-151 writes through stb/tinyexr; here): PNG, BMP, TGA and PPM
+ * (8-bit RGB), PFM and OpenEXR (float RGB). Input rows are bottom-first as the frame buffers;
+ * PNG, BMP, TGA and PPM show the image upright (the reference flips on write; BMP and TGA store
+ * rows bottom-up), PFM stores rows bottom-first as the format wants, and EXR stores the rows in
+ * the order given, as the reference's SaveFrameEXR does with the GL buffer (Export.h:56-151:
+ * channels B, G, R as 32-bit float; written here without compression). TGA is run-length
+ * encoded (stb_image_write's default). */
 lf_status lf_write_png(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
+lf_status lf_write_bmp(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
+lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_pfm(const char* path, const float* rgbf, int32_t width, int32_t height);
+lf_status lf_write_exr(const char* path, const float* rgbf, int32_t width, int32_t height);
 
 /* Render without allocating (no counterpart in the reference). For callers that cannot
  * allocate device memory while rendering - plugin hosts that hand out a fixed arena,

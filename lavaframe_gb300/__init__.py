@@ -100,6 +100,9 @@ _SIG = {
     "lf_write_png": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "lf_write_ppm": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "lf_write_pfm": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32]),
+    "lf_write_bmp": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
+    "lf_write_tga": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
+    "lf_write_exr": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32]),
     "lf_server_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
     "lf_server_remove_scene": (C.c_int, [_P, C.c_int64]),
@@ -440,15 +443,18 @@ class PostParams(C.Structure):
 
 
 def write_image(path, img):
-    """PNG / PPM from (H, W, 3) uint8, PFM from float32; row 0 = bottom."""
+    """PNG / BMP / TGA / PPM from (H, W, 3) uint8, PFM / EXR from float32, chosen by the file
+    extension (PNG otherwise); row 0 = bottom."""
     path = str(path)
     h, w = img.shape[:2]
-    if path.endswith(".pfm"):
+    ext = path.rsplit(".", 1)[-1].lower()
+    if ext in ("pfm", "exr"):
         a = np.ascontiguousarray(img, np.float32)
-        _chk(lib().lf_write_pfm(path.encode(), _fp(a), w, h))
+        fn = lib().lf_write_exr if ext == "exr" else lib().lf_write_pfm
+        _chk(fn(path.encode(), _fp(a), w, h))
     else:
         a = np.ascontiguousarray(img, np.uint8)
-        fn = lib().lf_write_ppm if path.endswith(".ppm") else lib().lf_write_png
+        fn = {"ppm": lib().lf_write_ppm, "bmp": lib().lf_write_bmp, "tga": lib().lf_write_tga}.get(ext, lib().lf_write_png)
         _chk(fn(path.encode(), a.ctypes.data_as(_P), w, h))
 
 

@@ -1,6 +1,8 @@
 // Image export: PNG (zlib stream of stored deflate blocks, CRC-32 and Adler-32 per the PNG and
-// zlib specifications), binary PPM and PFM. Replaces the stb_image_write / tinyexr calls of
-// Export.h:14-151 for the formats a headless render needs.
+// zlib specifications), BMP (24-bit, uncompressed), TGA (run-length encoded true colour, the
+// form stb_image_write writes by default), OpenEXR (single-part scanline, 32-bit float B, G, R
+// channels, no compression), binary PPM and PFM. Replaces the stb_image_write / tinyexr calls
+// of Export.h:14-151 (JPG and tinyexr's compressors are not written here).
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -45,6 +47,27 @@ void chunk(std::vector<uint8_t>& out, const char* type, const std::vector<uint8_
     td.insert(td.end(), data.begin(), data.end());
     out.insert(out.end(), td.begin(), td.end());
     put32(out, crc32(td.data(), td.size()));
+}
+
+void put_le(std::vector<uint8_t>& v, uint64_t x, int bytes)
+{
+    for (int k = 0; k < bytes; ++k) v.push_back((uint8_t)(x >> (8 * k)));
+}
+
+void put_f32(std::vector<uint8_t>& v, float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    put_le(v, u, 4);
+}
+
+// OpenEXR header attribute: name, type name, byte size, value
+void exr_attr(std::vector<uint8_t>& v, const char* name, const char* type, const std::vector<uint8_t>& value)
+{
+    v.insert(v.end(), name, name + std::strlen(name) + 1);
+    v.insert(v.end(), type, type + std::strlen(type) + 1);
+    put_le(v, value.size(), 4);
+    v.insert(v.end(), value.begin(), value.end());
 }
 
 bool write_file(const char* path, const void* data, size_t n)
@@ -101,6 +124,136 @@ lf_status lf_write_png(const char* path, const uint8_t* rgb8, int32_t w, int32_t
     chunk(png, "IDAT", z);
     chunk(png, "IEND", {});
     return write_file(path, png.data(), png.size()) ? LF_OK : LF_ERR_IO;
+}
+
+lf_status lf_write_bmp(const char* path, const uint8_t* rgb8, int32_t w, int32_t h)
+{
+    if (!path || !rgb8 || w <= 0 || h <= 0) return LF_ERR_INVALID;
+    const size_t stride = ((size_t)w * 3 + 3) / 4 * 4;   // rows padded to 4 bytes
+    const size_t pixels = stride * h;
+    std::vector<uint8_t> out;
+    out.reserve(54 + pixels);
+    // BITMAPFILEHEADER
+    out.push_back('B');
+    out.push_back('M');
+    put_le(out, 54 + pixels, 4);
+    put_le(out, 0, 4);
+    put_le(out, 54, 4);
+    // BITMAPINFOHEADER: positive height = rows stored bottom-up, 24 bits, BI_RGB
+    put_le(out, 40, 4);
+    put_le(out, (uint32_t)w, 4);
+    put_le(out, (uint32_t)h, 4);
+    put_le(out, 1, 2);
+    put_le(out, 24, 2);
+    put_le(out, 0, 4);
+    put_le(out, pixels, 4);
+    put_le(out, 2835, 4);   // 72 dpi
+    put_le(out, 2835, 4);
+    put_le(out, 0, 4);
+    put_le(out, 0, 4);
+    for (int y = 0; y < h; ++y)   // the input's bottom row first, as BMP stores it
+    {
+        const uint8_t* row = rgb8 + (size_t)y * w * 3;
+        for (int x = 0; x < w; ++x)
+        {
+            out.push_back(row[x * 3 + 2]);
+            out.push_back(row[x * 3 + 1]);
+            out.push_back(row[x * 3 + 0]);
+        }
+        for (size_t k = (size_t)w * 3; k < stride; ++k) out.push_back(0);
+    }
+    return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
+}
+
+lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t w, int32_t h)
+{
+    if (!path || !rgb8 || w <= 0 || h <= 0 || w > 65535 || h > 65535) return LF_ERR_INVALID;
+    std::vector<uint8_t> out;
+    // header: no id, no colour map, type 10 (run-length true colour), origin bottom left
+    const uint8_t hdr[18] = {0, 0, 10, 0, 0, 0, 0, 0, 0, 0, 0, 0, (uint8_t)w, (uint8_t)(w >> 8), (uint8_t)h,
+                             (uint8_t)(h >> 8), 24, 0};
+    out.insert(out.end(), hdr, hdr + 18);
+    auto px = [&](const uint8_t* p) {
+        out.push_back(p[2]);
+        out.push_back(p[1]);
+        out.push_back(p[0]);
+    };
+    for (int y = 0; y < h; ++y)   // bottom row first; packets never cross a row
+    {
+        const uint8_t* row = rgb8 + (size_t)y * w * 3;
+        int x = 0;
+        while (x < w)
+        {
+            int run = 1;   // equal pixels from x
+            while (x + run < w && run < 128 && std::memcmp(row + (x + run) * 3, row + x * 3, 3) == 0) ++run;
+            if (run > 1)
+            {
+                out.push_back((uint8_t)(0x80 | (run - 1)));
+                px(row + x * 3);
+                x += run;
+                continue;
+            }
+            int lit = 1;   // pixels up to the next pair of equal ones
+            while (x + lit < w && lit < 128 &&
+                   !(x + lit + 1 < w && std::memcmp(row + (x + lit) * 3, row + (x + lit + 1) * 3, 3) == 0))
+                ++lit;
+            out.push_back((uint8_t)(lit - 1));
+            for (int k = 0; k < lit; ++k) px(row + (x + k) * 3);
+            x += lit;
+        }
+    }
+    const char footer[] = "\0\0\0\0\0\0\0\0TRUEVISION-XFILE.";   // TGA 2.0: no extension or developer area
+    out.insert(out.end(), footer, footer + sizeof footer);
+    return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
+}
+
+lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h)
+{
+    if (!path || !rgbf || w <= 0 || h <= 0) return LF_ERR_INVALID;
+    std::vector<uint8_t> out{0x76, 0x2f, 0x31, 0x01, 2, 0, 0, 0};   // magic, version 2, scanline
+    std::vector<uint8_t> v;
+    for (const char* c : {"B", "G", "R"})   // channel list in name order, 32-bit float, 1x1 sampling
+    {
+        v.push_back((uint8_t)c[0]);
+        v.push_back(0);
+        put_le(v, 2, 4);
+        put_le(v, 0, 4);   // pLinear + reserved
+        put_le(v, 1, 4);
+        put_le(v, 1, 4);
+    }
+    v.push_back(0);
+    exr_attr(out, "channels", "chlist", v);
+    exr_attr(out, "compression", "compression", {0});
+    v.clear();
+    for (int32_t k : {0, 0, w - 1, h - 1}) put_le(v, (uint32_t)k, 4);
+    exr_attr(out, "dataWindow", "box2i", v);
+    exr_attr(out, "displayWindow", "box2i", v);
+    exr_attr(out, "lineOrder", "lineOrder", {0});
+    v.clear();
+    put_f32(v, 1.0f);
+    exr_attr(out, "pixelAspectRatio", "float", v);
+    v.clear();
+    put_f32(v, 0.0f);
+    put_f32(v, 0.0f);
+    exr_attr(out, "screenWindowCenter", "v2f", v);
+    v.clear();
+    put_f32(v, 1.0f);
+    exr_attr(out, "screenWindowWidth", "float", v);
+    out.push_back(0);
+    // one scanline per block: the offset table, then y, byte count and the B, G and R rows.
+    // Rows go out in the order given (the reference writes the bottom-first GL buffer as is).
+    const size_t rowBytes = (size_t)w * 3 * 4;
+    const size_t table = out.size();
+    for (int y = 0; y < h; ++y) put_le(out, table + (size_t)h * 8 + (size_t)y * (8 + rowBytes), 8);
+    for (int y = 0; y < h; ++y)
+    {
+        put_le(out, (uint32_t)y, 4);
+        put_le(out, rowBytes, 4);
+        const float* row = rgbf + (size_t)y * w * 3;
+        for (int c = 2; c >= 0; --c)
+            for (int x = 0; x < w; ++x) put_f32(out, row[x * 3 + c]);
+    }
+    return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
 }
 
 lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t w, int32_t h)

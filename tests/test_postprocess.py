@@ -122,6 +122,92 @@ def test_png_and_pfm_writers_round_trip(tmp_path):
     assert np.array_equal(np.frombuffer(raw[len(hdr):], "<f4").reshape(5, 7, 3), imgf)
 
 
+def read_bmp(path):
+    """24-bit BI_RGB reader (BITMAPFILEHEADER + BITMAPINFOHEADER), rows returned bottom-first."""
+    data = open(path, "rb").read()
+    assert data[:2] == b"BM" and struct.unpack("<I", data[2:6])[0] == len(data)
+    off, hsize, w, h, planes, bpp, comp = struct.unpack("<I I i i H H I", data[10:34])
+    assert (hsize, planes, bpp, comp) == (40, 1, 24, 0) and h > 0
+    stride = (3 * w + 3) // 4 * 4
+    rows = [np.frombuffer(data[off + y * stride: off + y * stride + 3 * w], np.uint8).reshape(w, 3)[:, ::-1]
+            for y in range(h)]
+    return np.stack(rows)
+
+
+def read_tga(path):
+    """Type-10 (run-length true colour, 24-bit) reader, rows returned bottom-first."""
+    data = open(path, "rb").read()
+    idlen, cmtype, typ = data[0], data[1], data[2]
+    w, h, bpp, desc = struct.unpack("<HHBB", data[12:18])
+    assert (cmtype, typ, bpp) == (0, 10, 24) and not desc & 0x20   # bottom-left origin
+    pos, px = 18 + idlen, []
+    while len(px) < w * h:
+        c = data[pos]
+        pos += 1
+        n = (c & 0x7F) + 1
+        if c & 0x80:
+            px += [data[pos:pos + 3]] * n
+            pos += 3
+        else:
+            px += [data[pos + 3 * k:pos + 3 * k + 3] for k in range(n)]
+            pos += 3 * n
+    assert len(px) == w * h and data[pos:] == b"\0" * 8 + b"TRUEVISION-XFILE.\0"
+    return np.frombuffer(b"".join(px), np.uint8).reshape(h, w, 3)[:, :, ::-1]
+
+
+def read_exr(path):
+    """Single-part scanline OpenEXR reader for uncompressed 32-bit float channels."""
+    data = open(path, "rb").read()
+    assert data[:4] == bytes([0x76, 0x2F, 0x31, 0x01]) and data[4] == 2
+    pos, attrs = 8, {}
+    while data[pos] != 0:
+        name_end = data.index(0, pos)
+        type_end = data.index(0, name_end + 1)
+        size = struct.unpack("<i", data[type_end + 1:type_end + 5])[0]
+        attrs[data[pos:name_end].decode()] = (data[name_end + 1:type_end].decode(),
+                                                data[type_end + 5:type_end + 5 + size])
+        pos = type_end + 5 + size
+    pos += 1
+    assert attrs["compression"] == ("compression", b"\0")
+    ch, chans = attrs["channels"][1], []
+    i = 0
+    while ch[i] != 0:
+        e = ch.index(0, i)
+        ptype, _, xs, ys = struct.unpack("<iiii", ch[e + 1:e + 17])
+        assert ptype == 2 and xs == ys == 1
+        chans.append(ch[i:e].decode())
+        i = e + 17
+    x0, y0, x1, y1 = struct.unpack("<iiii", attrs["dataWindow"][1])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    offsets = struct.unpack(f"<{h}Q", data[pos:pos + 8 * h])
+    img = np.zeros((h, w, len(chans)), np.float32)
+    for off in offsets:
+        y, n = struct.unpack("<ii", data[off:off + 8])
+        assert n == 4 * w * len(chans)
+        row = np.frombuffer(data[off + 8:off + 8 + n], "<f4").reshape(len(chans), w)
+        img[y - y0] = row.T
+    return chans, img
+
+
+def test_bmp_tga_exr_writers_round_trip(tmp_path):
+    rng = np.random.default_rng(2)
+    for h, w in ((5, 7), (33, 130)):   # odd widths: BMP row padding; TGA packets within rows
+        img8 = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+        img8[1, 2:40] = (10, 20, 30)                 # runs for the TGA run-length packets
+        img8[-1] = 255
+        lf.write_image(tmp_path / "a.bmp", img8)
+        assert np.array_equal(read_bmp(tmp_path / "a.bmp"), img8)   # stored bottom-up
+        lf.write_image(tmp_path / "a.tga", img8)
+        assert np.array_equal(read_tga(tmp_path / "a.tga"), img8)
+        imgf = rng.normal(size=(h, w, 3)).astype(np.float32)
+        imgf[0, 0] = (np.inf, -0.0, 1e-40)
+        lf.write_image(tmp_path / "a.exr", imgf)
+        chans, back = read_exr(tmp_path / "a.exr")
+        assert chans == ["B", "G", "R"]
+        # rows in the order given, channels by name: bit for bit
+        assert back[:, :, ::-1].tobytes() == imgf.tobytes()
+
+
 @pytest.mark.gpu
 def test_gpu_postprocess_is_bit_exact(ctx):
     s = scenes.build("cornell")
