@@ -301,7 +301,7 @@ typedef struct lf_post_params
 /* rgb8 (W*H*3 bytes) and/or rgbf (W*H*3 floats, after tone map and vignette, before the
  * 8-bit conversion); row 0 = bottom as in GL. `samples` = the accumulated sample count. */
 lf_status lf_frame_postprocess(lf_frame* f, const lf_post_params* p, int32_t samples, uint8_t* rgb8, float* rgbf);
-/* Image export (Export.h:14-151 writes through stb/tinyexr; here): PNG, BMP, TGA and PPM
+/* Image export (Export.h:14-151 writes through stb/tinyexr; here): PNG, BMP, TGA, JPEG and PPM
  * (8-bit RGB), PFM and OpenEXR (float RGB). Input rows are bottom-first as the frame buffers;
  * PNG, BMP, TGA and PPM show the image upright (the reference flips on write; BMP and TGA store
  * rows bottom-up), PFM stores rows bottom-first as the format wants, and EXR stores the rows in
@@ -314,6 +314,9 @@ lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t width, int
 lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_pfm(const char* path, const float* rgbf, int32_t width, int32_t height);
 lf_status lf_write_exr(const char* path, const float* rgbf, int32_t width, int32_t height);
+/* Baseline JPEG (SaveFrameJPG, Export.h:37-46): `quality` 1..100 scales the quantisation
+ * tables; 4:4:4 YCbCr; Huffman tables built for the image. Shown upright like PNG. */
+lf_status lf_write_jpg(const char* path, const uint8_t* rgb8, int32_t width, int32_t height, int32_t quality);
 
 /* Render without allocating (no counterpart in the reference). For callers that cannot
  * allocate device memory while rendering - plugin hosts that hand out a fixed arena,

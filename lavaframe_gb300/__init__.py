@@ -103,6 +103,7 @@ _SIG = {
     "lf_write_bmp": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "lf_write_tga": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "lf_write_exr": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32]),
+    "lf_write_jpg": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32, C.c_int32]),
     "lf_server_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
     "lf_server_remove_scene": (C.c_int, [_P, C.c_int64]),
@@ -442,9 +443,9 @@ class PostParams(C.Structure):
         return cls(tonemap, 0, 0, 0, 0, 0.05, 5.0, -0.5, 0.5, 0.0, 1.0)
 
 
-def write_image(path, img):
-    """PNG / BMP / TGA / PPM from (H, W, 3) uint8, PFM / EXR from float32, chosen by the file
-    extension (PNG otherwise); row 0 = bottom."""
+def write_image(path, img, jpg_quality=90):
+    """PNG / BMP / TGA / JPEG / PPM from (H, W, 3) uint8, PFM / EXR from float32, chosen by the
+    file extension (PNG otherwise); row 0 = bottom."""
     path = str(path)
     h, w = img.shape[:2]
     ext = path.rsplit(".", 1)[-1].lower()
@@ -454,6 +455,9 @@ def write_image(path, img):
         _chk(fn(path.encode(), _fp(a), w, h))
     else:
         a = np.ascontiguousarray(img, np.uint8)
+        if ext in ("jpg", "jpeg"):
+            _chk(lib().lf_write_jpg(path.encode(), a.ctypes.data_as(_P), w, h, int(jpg_quality)))
+            return
         fn = {"ppm": lib().lf_write_ppm, "bmp": lib().lf_write_bmp, "tga": lib().lf_write_tga}.get(ext, lib().lf_write_png)
         _chk(fn(path.encode(), a.ctypes.data_as(_P), w, h))
 

@@ -1,9 +1,12 @@
 // Image export: PNG (zlib stream of stored deflate blocks, CRC-32 and Adler-32 per the PNG and
 // zlib specifications), BMP (24-bit, uncompressed), TGA (run-length encoded true colour, the
 // form stb_image_write writes by default), OpenEXR (single-part scanline, 32-bit float B, G, R
-// channels, no compression), binary PPM and PFM. Replaces the stb_image_write / tinyexr calls
-// of Export.h:14-151 (JPG and tinyexr's compressors are not written here).
+// channels, no compression), baseline JPEG (ITU-T T.81: 4:4:4 YCbCr, quality-scaled Annex K
+// quantisation tables, Huffman tables built for each image by the Annex K.2 procedure), binary
+// PPM and PFM. Replaces the stb_image_write / tinyexr calls of Export.h:14-151 (tinyexr's
+// compressors are not written here).
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -68,6 +71,146 @@ void exr_attr(std::vector<uint8_t>& v, const char* name, const char* type, const
     v.insert(v.end(), type, type + std::strlen(type) + 1);
     put_le(v, value.size(), 4);
     v.insert(v.end(), value.begin(), value.end());
+}
+
+// ---------------------------------------------------------------- baseline JPEG (ITU-T T.81)
+// Example quantisation tables of T.81 Annex K.1 (natural order), scaled by quality the way the
+// IJG library does: scale = 5000 / q below 50, 200 - 2 q from there.
+const uint8_t kLumaQ[64] = {16, 11, 10, 16, 24,  40,  51,  61,  12, 12, 14, 19, 26,  58,  60,  55,
+                            14, 13, 16, 24, 40,  57,  69,  56,  14, 17, 22, 29, 51,  87,  80,  62,
+                            18, 22, 37, 56, 68,  109, 103, 77,  24, 35, 55, 64, 81,  104, 113, 92,
+                            49, 64, 78, 87, 103, 121, 120, 101, 72, 92, 95, 98, 112, 100, 103, 99};
+const uint8_t kChromaQ[64] = {17, 18, 24, 47, 99, 99, 99, 99, 18, 21, 26, 66, 99, 99, 99, 99,
+                              24, 26, 56, 99, 99, 99, 99, 99, 47, 66, 99, 99, 99, 99, 99, 99,
+                              99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99,
+                              99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99};
+
+// zigzag position k -> natural index (row * 8 + column)
+void zigzag(int zz[64])
+{
+    int k = 0;
+    for (int s = 0; s < 15; ++s)
+        for (int i = 0; i < 8; ++i)
+        {
+            const int r = (s % 2) ? i : s - i;   // odd diagonals run down-left, even ones up-right
+            const int c = s - r;
+            if (r < 0 || r > 7 || c < 0 || c > 7) continue;
+            zz[k++] = r * 8 + c;
+        }
+}
+
+int category(int v)
+{
+    int a = v < 0 ? -v : v, n = 0;
+    while (a) { ++n; a >>= 1; }
+    return n;
+}
+
+// Code lengths for the symbols with nonzero counts (Annex K.2: Huffman procedure with one
+// reserved code point so that no code is all ones, lengths limited to 16 bits), returned as
+// the DHT BITS / HUFFVAL lists and per-symbol code and length.
+struct HuffTable
+{
+    uint8_t bits[17] = {};
+    std::vector<uint8_t> vals;
+    uint16_t code[256] = {};
+    uint8_t len[256] = {};
+};
+
+void build_huffman(const uint32_t freqIn[256], HuffTable& t)
+{
+    long long freq[257];
+    int codesize[257], others[257];
+    for (int i = 0; i < 256; ++i) freq[i] = freqIn[i];
+    freq[256] = 1;   // reserved point
+    for (int i = 0; i < 257; ++i)
+    {
+        codesize[i] = 0;
+        others[i] = -1;
+    }
+    while (true)   // Figure K.1
+    {
+        int v1 = -1, v2 = -1;
+        for (int i = 0; i < 257; ++i)
+            if (freq[i] > 0 && (v1 < 0 || freq[i] <= freq[v1])) v1 = i;
+        for (int i = 0; i < 257; ++i)
+            if (freq[i] > 0 && i != v1 && (v2 < 0 || freq[i] <= freq[v2])) v2 = i;
+        if (v2 < 0) break;
+        freq[v1] += freq[v2];
+        freq[v2] = 0;
+        for (++codesize[v1]; others[v1] >= 0; ++codesize[v1]) v1 = others[v1];
+        others[v1] = v2;
+        for (++codesize[v2]; others[v2] >= 0; ++codesize[v2]) v2 = others[v2];
+    }
+    int bits[258] = {};   // code sizes reach at most 256 with 257 points
+    for (int i = 0; i < 257; ++i)
+        if (codesize[i]) ++bits[codesize[i]];
+    for (int i = 257; i > 16; --i)   // Figure K.3: limit to 16 bits
+        while (bits[i] > 0)
+        {
+            int j = i - 2;
+            while (bits[j] == 0) --j;
+            bits[i] -= 2;
+            ++bits[i - 1];
+            bits[j + 1] += 2;
+            --bits[j];
+        }
+    int last = 16;
+    while (bits[last] == 0) --last;
+    --bits[last];   // drop the reserved point
+    // symbols by code size, then value (Figure K.4); the reserved point sorts last
+    t.vals.clear();
+    for (int size = 1; size <= 257; ++size)
+        for (int i = 0; i < 256; ++i)
+            if (codesize[i] == size) t.vals.push_back((uint8_t)i);
+    for (int i = 1; i <= 16; ++i) t.bits[i] = (uint8_t)bits[i];
+    // canonical codes (Annex C)
+    int k = 0;
+    uint16_t code = 0;
+    for (int l = 1; l <= 16; ++l)
+    {
+        for (int n = 0; n < bits[l]; ++n, ++k)
+        {
+            t.code[t.vals[k]] = code++;
+            t.len[t.vals[k]] = (uint8_t)l;
+        }
+        code <<= 1;
+    }
+    t.vals.resize(k);
+}
+
+struct BitWriter
+{
+    std::vector<uint8_t>& out;
+    uint32_t acc = 0;
+    int n = 0;
+    void put(uint32_t bits, int len)
+    {
+        for (int i = len - 1; i >= 0; --i)
+        {
+            acc = (acc << 1) | ((bits >> i) & 1u);
+            if (++n == 8)
+            {
+                out.push_back((uint8_t)acc);
+                if (acc == 0xFF) out.push_back(0);   // byte stuffing
+                acc = 0;
+                n = 0;
+            }
+        }
+    }
+    void flush()
+    {
+        while (n) put(1, 1);   // pad with ones
+    }
+};
+
+void marker(std::vector<uint8_t>& o, uint8_t m, const std::vector<uint8_t>& body)
+{
+    o.push_back(0xFF);
+    o.push_back(m);
+    o.push_back((uint8_t)((body.size() + 2) >> 8));
+    o.push_back((uint8_t)(body.size() + 2));
+    o.insert(o.end(), body.begin(), body.end());
 }
 
 bool write_file(const char* path, const void* data, size_t n)
@@ -254,6 +397,131 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
             for (int x = 0; x < w; ++x) put_f32(out, row[x * 3 + c]);
     }
     return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
+}
+
+lf_status lf_write_jpg(const char* path, const uint8_t* rgb8, int32_t w, int32_t h, int32_t quality)
+{
+    if (!path || !rgb8 || w <= 0 || h <= 0 || w > 65535 || h > 65535) return LF_ERR_INVALID;
+    const int q = std::max(1, std::min(100, quality));
+    const int scale = q < 50 ? 5000 / q : 200 - 2 * q;
+    int zz[64];
+    zigzag(zz);
+    uint8_t qt[2][64];
+    for (int i = 0; i < 64; ++i)
+    {
+        qt[0][i] = (uint8_t)std::max(1, std::min(255, (kLumaQ[i] * scale + 50) / 100));
+        qt[1][i] = (uint8_t)std::max(1, std::min(255, (kChromaQ[i] * scale + 50) / 100));
+    }
+    double cosv[8][8];
+    for (int x = 0; x < 8; ++x)
+        for (int u = 0; u < 8; ++u) cosv[x][u] = std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0);
+    // quantised coefficients of every block, zigzag order; components interleaved per block
+    const int bw = (w + 7) / 8, bh = (h + 7) / 8;
+    std::vector<int16_t> coef((size_t)bw * bh * 3 * 64);
+    for (int by = 0; by < bh; ++by)
+        for (int bx = 0; bx < bw; ++bx)
+        {
+            double ycc[3][64];
+            for (int y = 0; y < 8; ++y)
+                for (int x = 0; x < 8; ++x)
+                {
+                    // JPEG rows run top down; the input's row 0 is the bottom. Edges repeat.
+                    const int iy = std::min(h - 1, by * 8 + y), ix = std::min(w - 1, bx * 8 + x);
+                    const uint8_t* p = rgb8 + ((size_t)(h - 1 - iy) * w + ix) * 3;
+                    const double r = p[0], g = p[1], b = p[2];
+                    ycc[0][y * 8 + x] = 0.299 * r + 0.587 * g + 0.114 * b - 128.0;   // JFIF YCbCr, level shift
+                    ycc[1][y * 8 + x] = -0.168736 * r - 0.331264 * g + 0.5 * b;
+                    ycc[2][y * 8 + x] = 0.5 * r - 0.418688 * g - 0.081312 * b;
+                }
+            for (int c = 0; c < 3; ++c)
+            {
+                // separable DCT-II: along rows (x -> u), then along columns (y -> v)
+                double row[8][8], dct[8][8];
+                for (int y = 0; y < 8; ++y)
+                    for (int u = 0; u < 8; ++u)
+                    {
+                        double sum = 0.0;
+                        for (int x = 0; x < 8; ++x) sum += ycc[c][y * 8 + x] * cosv[x][u];
+                        row[y][u] = sum;
+                    }
+                for (int v = 0; v < 8; ++v)
+                    for (int u = 0; u < 8; ++u)
+                    {
+                        double sum = 0.0;
+                        for (int y = 0; y < 8; ++y) sum += row[y][u] * cosv[y][v];
+                        const double cu = u ? 1.0 : 1.0 / std::sqrt(2.0), cv = v ? 1.0 : 1.0 / std::sqrt(2.0);
+                        dct[v][u] = 0.25 * cu * cv * sum;
+                    }
+                int16_t* out = &coef[(((size_t)by * bw + bx) * 3 + c) * 64];
+                for (int k = 0; k < 64; ++k)
+                    out[k] = (int16_t)std::lround(dct[zz[k] >> 3][zz[k] & 7] / qt[c ? 1 : 0][zz[k]]);
+            }
+        }
+    // symbol statistics, then Huffman tables (DC and AC for luma and for chroma)
+    uint32_t freq[4][256] = {};
+    auto walk = [&](auto&& emit) {
+        int pred[3] = {0, 0, 0};
+        for (size_t blk = 0; blk < (size_t)bw * bh; ++blk)
+            for (int c = 0; c < 3; ++c)
+            {
+                const int16_t* cf = &coef[(blk * 3 + c) * 64];
+                const int t = c ? 1 : 0;
+                const int diff = cf[0] - pred[c];
+                pred[c] = cf[0];
+                emit(t * 2, category(diff), diff);
+                int run = 0;
+                for (int k = 1; k < 64; ++k)
+                {
+                    if (cf[k] == 0)
+                    {
+                        ++run;
+                        continue;
+                    }
+                    while (run > 15)
+                    {
+                        emit(t * 2 + 1, 0xF0, 0);   // ZRL
+                        run -= 16;
+                    }
+                    const int sz = category(cf[k]);
+                    emit(t * 2 + 1, (run << 4) | sz, cf[k]);
+                    run = 0;
+                }
+                if (run) emit(t * 2 + 1, 0x00, 0);   // EOB
+            }
+    };
+    walk([&](int table, int sym, int) { ++freq[table][sym]; });
+    HuffTable ht[4];
+    for (int i = 0; i < 4; ++i) build_huffman(freq[i], ht[i]);
+
+    std::vector<uint8_t> o{0xFF, 0xD8};
+    marker(o, 0xE0, {'J', 'F', 'I', 'F', 0, 1, 1, 0, 0, 1, 0, 1, 0, 0});   // JFIF 1.01, aspect 1:1
+    for (int t = 0; t < 2; ++t)
+    {
+        std::vector<uint8_t> body{(uint8_t)t};
+        for (int k = 0; k < 64; ++k) body.push_back(qt[t][zz[k]]);
+        marker(o, 0xDB, body);
+    }
+    marker(o, 0xC0, {8, (uint8_t)(h >> 8), (uint8_t)h, (uint8_t)(w >> 8), (uint8_t)w, 3, 1, 0x11, 0, 2, 0x11, 1, 3,
+                     0x11, 1});
+    const uint8_t classId[4] = {0x00, 0x10, 0x01, 0x11};   // DC luma, AC luma, DC chroma, AC chroma
+    for (int i = 0; i < 4; ++i)
+    {
+        std::vector<uint8_t> body{classId[i]};
+        body.insert(body.end(), ht[i].bits + 1, ht[i].bits + 17);
+        body.insert(body.end(), ht[i].vals.begin(), ht[i].vals.end());
+        marker(o, 0xC4, body);
+    }
+    marker(o, 0xDA, {3, 1, 0x00, 2, 0x11, 3, 0x11, 0, 63, 0});
+    BitWriter bw8{o};
+    walk([&](int table, int sym, int v) {
+        bw8.put(ht[table].code[sym], ht[table].len[sym]);
+        const int sz = (table & 1) ? (sym & 15) : sym;
+        if (sz) bw8.put((uint32_t)(v < 0 ? v - 1 : v) & ((1u << sz) - 1u), sz);
+    });
+    bw8.flush();
+    o.push_back(0xFF);
+    o.push_back(0xD9);
+    return write_file(path, o.data(), o.size()) ? LF_OK : LF_ERR_IO;
 }
 
 lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t w, int32_t h)

@@ -208,6 +208,122 @@ def test_bmp_tga_exr_writers_round_trip(tmp_path):
         assert back[:, :, ::-1].tobytes() == imgf.tobytes()
 
 
+def read_jpg(path):
+    """Baseline sequential JPEG decoder (ITU-T T.81, 8-bit, 1x1 sampling), rows returned top down."""
+    data = open(path, "rb").read()
+    assert data[:2] == b"\xff\xd8"
+    pos, qt, huff, comps, scan = 2, {}, {}, None, None
+    while True:
+        assert data[pos] == 0xFF
+        m = data[pos + 1]
+        pos += 2
+        if m == 0xD9:
+            break
+        n = struct.unpack(">H", data[pos:pos + 2])[0]
+        seg = data[pos + 2:pos + n]
+        pos += n
+        if m == 0xDB:
+            i = 0
+            while i < len(seg):
+                assert seg[i] >> 4 == 0
+                qt[seg[i] & 15] = np.frombuffer(seg[i + 1:i + 65], np.uint8).astype(np.float64)
+                i += 65
+        elif m == 0xC0:
+            assert seg[0] == 8
+            h, w = struct.unpack(">HH", seg[1:5])
+            comps = [(seg[6 + 3 * k], seg[7 + 3 * k], seg[8 + 3 * k]) for k in range(seg[5])]
+            assert all(c[1] == 0x11 for c in comps)
+        elif m == 0xC4:
+            i = 0
+            while i < len(seg):
+                bits, k, code, table = seg[i + 1:i + 17], 0, 0, {}
+                vals = seg[i + 17:i + 17 + sum(bits)]
+                for length in range(1, 17):
+                    for _ in range(bits[length - 1]):
+                        table[(length, code)] = vals[k]
+                        code, k = code + 1, k + 1
+                    code <<= 1
+                huff[seg[i]] = table
+                i += 17 + sum(bits)
+        elif m == 0xDA:
+            scan = [(seg[1 + 2 * k], seg[2 + 2 * k]) for k in range(seg[0])]
+            end = pos
+            while not (data[end] == 0xFF and data[end + 1] != 0):
+                end += 1
+            ecs = data[pos:end].replace(b"\xff\x00", b"\xff")
+            pos = end
+    bitstr = "".join(f"{b:08b}" for b in ecs)
+    bp = 0
+
+    def receive(nbits):
+        nonlocal bp
+        v = int(bitstr[bp:bp + nbits], 2) if nbits else 0
+        bp += nbits
+        return v
+
+    def decode(table):
+        code = 0
+        for length in range(1, 17):
+            code = (code << 1) | receive(1)
+            if (length, code) in table:
+                return table[(length, code)]
+        raise AssertionError("bad Huffman code")
+
+    def extend(v, t):
+        return v - (1 << t) + 1 if t and v < (1 << (t - 1)) else v
+
+    order = sorted(range(64), key=lambda i: (i // 8 + i % 8, i // 8 if (i // 8 + i % 8) % 2 else -(i // 8)))
+    cu = np.array([np.sqrt(0.5)] + [1.0] * 7)
+    M = np.array([[cu[u] / 2 * np.cos((2 * x + 1) * u * np.pi / 16) for x in range(8)] for u in range(8)])
+    bw, bh = (w + 7) // 8, (h + 7) // 8
+    planes = np.zeros((3, bh * 8, bw * 8))
+    pred = [0, 0, 0]
+    qsel = {c[0]: c[2] for c in comps}
+    for by in range(bh):
+        for bx in range(bw):
+            for ci, (cid, tables) in enumerate(scan):
+                coef = np.zeros(64)
+                t = decode(huff[0x00 | (tables >> 4)])
+                pred[ci] += extend(receive(t), t)
+                coef[0] = pred[ci]
+                k = 1
+                while k < 64:
+                    rs = decode(huff[0x10 | (tables & 15)])
+                    r, sz = rs >> 4, rs & 15
+                    if sz == 0:
+                        if r != 15:
+                            break
+                        k += 16
+                        continue
+                    k += r
+                    coef[k] = extend(receive(sz), sz)
+                    k += 1
+                F = np.zeros(64)
+                F[order] = coef * qt[qsel[cid]]
+                planes[ci, by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] = M.T @ F.reshape(8, 8) @ M
+    Y, Cb, Cr = planes[0] + 128, planes[1], planes[2]
+    rgb = np.stack([Y + 1.402 * Cr, Y - 0.344136 * Cb - 0.714136 * Cr, Y + 1.772 * Cb], -1)
+    return np.clip(np.rint(rgb), 0, 255)[:h, :w]
+
+
+def test_jpg_writer_decodes_to_the_image(tmp_path):
+    rng = np.random.default_rng(3)
+    for h, w in ((21, 37), (48, 64)):   # partial edge blocks, and whole ones
+        yy, xx = np.mgrid[0:h, 0:w]
+        smooth = np.stack([xx * 255 / w, yy * 255 / h, (xx + yy) * 127 / (w + h) + 60], -1)
+        img8 = np.clip(smooth + rng.normal(0, 3, smooth.shape), 0, 255).astype(np.uint8)
+        sizes = {}
+        for q in (50, 95, 100):
+            lf.write_image(tmp_path / f"a{q}.jpg", img8, jpg_quality=q)
+            sizes[q] = (tmp_path / f"a{q}.jpg").stat().st_size
+            back = read_jpg(tmp_path / f"a{q}.jpg")
+            err = np.abs(back - img8[::-1].astype(np.float64))   # shown upright: top row first
+            # noise of sigma 3 sits in the coefficients that quality 50 and 95 quantise
+            assert err.mean() < {50: 4.0, 95: 3.0, 100: 0.5}[q], (q, err.mean())
+            assert err.max() <= {50: 25, 95: 16, 100: 3}[q], (q, err.max())
+        assert sizes[50] < sizes[95] < sizes[100]
+
+
 @pytest.mark.gpu
 def test_gpu_postprocess_is_bit_exact(ctx):
     s = scenes.build("cornell")
