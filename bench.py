@@ -593,7 +593,8 @@ def main():
             "cpu_baseline": {"value": cpu_v, "unit": "Grays/s", "cores": cores, "kind": "port",
                              "sample": f"{sample} of the 2^{args.rays_log2} rays, {cpu_dt:.1f} s"},
             "clocks": clk.summary(),
-            "gpu_launches": args.steps,
+            # per binned query: ray_keys, the three bin-scan kernels, ray_scatter, traversal
+            "gpu_launches": args.steps * 6,
             "extra": extra,
         }
         print(json.dumps(line), flush=True)
