@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -257,8 +258,10 @@ int32_t lf_hscene_add_mesh_file(lf_hscene* s, const char* path)
 int32_t lf_hscene_add_material(lf_hscene* s, const float* m28)
 {
     if (!s || !m28) return -1;
+    static_assert(std::is_trivially_copyable<Material>::value && sizeof(Material) == 28 * sizeof(float),
+                  "Material is the 112-byte float record");
     Material m;
-    std::memcpy(&m, m28, sizeof(Material));
+    std::memcpy(static_cast<void*>(&m), m28, sizeof(Material));
     return s->scene.AddMaterial(m);
 }
 
@@ -273,8 +276,10 @@ int32_t lf_hscene_add_instance(lf_hscene* s, int32_t mesh, const float* xf, int3
 int32_t lf_hscene_add_light(lf_hscene* s, const float* l15)
 {
     if (!s || !l15) return -1;
+    static_assert(std::is_trivially_copyable<Light>::value && sizeof(Light) == 15 * sizeof(float),
+                  "Light is the 60-byte float record");
     Light l;
-    std::memcpy(&l, l15, sizeof(Light));
+    std::memcpy(static_cast<void*>(&l), l15, sizeof(Light));
     return s->scene.AddLight(l);
 }
 
