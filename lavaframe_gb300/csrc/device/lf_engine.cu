@@ -130,7 +130,6 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
 // completions) and frees its slot.
 __global__ void engine_finish_kernel(EngineBuffers b, int parity)
 {
-    __shared__ int smem[33];
     __shared__ DoneTable table;
     EngineCtl* ctl = b.ctl;
     const int n = ctl->doneCount[parity];

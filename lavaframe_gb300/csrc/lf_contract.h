@@ -31,7 +31,7 @@
 // calls do.
 #if defined(__CUDACC__)
 #define LF_HD __host__ __device__ __forceinline__
-#define LF_HD_CALL static __host__ __device__ __noinline__
+#define LF_HD_CALL [[maybe_unused]] static __host__ __device__ __noinline__
 #else
 #define LF_HD inline
 #define LF_HD_CALL inline
