@@ -306,8 +306,8 @@ lf_status lf_frame_postprocess(lf_frame* f, const lf_post_params* p, int32_t sam
  * PNG, BMP, TGA and PPM show the image upright (the reference flips on write; BMP and TGA store
  * rows bottom-up), PFM stores rows bottom-first as the format wants, and EXR stores the rows in
  * the order given, as the reference's SaveFrameEXR does with the GL buffer (Export.h:56-151:
- * channels B, G, R as 32-bit float; written here without compression). TGA is run-length
- * encoded (stb_image_write's default). */
+ * channels B, G, R as 32-bit float, ZIP compression). TGA is run-length encoded
+ * (stb_image_write's default); PNG rows are filtered and deflated. */
 lf_status lf_write_png(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_bmp(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);

@@ -1,14 +1,16 @@
-// Image export: PNG (zlib stream of stored deflate blocks, CRC-32 and Adler-32 per the PNG and
+// Image export: PNG (row filters chosen per row, deflated; CRC-32 and Adler-32 per the PNG and
 // zlib specifications), BMP (24-bit, uncompressed), TGA (run-length encoded true colour, the
 // form stb_image_write writes by default), OpenEXR (single-part scanline, 32-bit float B, G, R
-// channels, no compression), baseline JPEG (ITU-T T.81: 4:4:4 YCbCr, quality-scaled Annex K
+// channels, ZIP compression as the reference's default), baseline JPEG (ITU-T T.81: 4:4:4 YCbCr, quality-scaled Annex K
 // quantisation tables, Huffman tables built for each image by the Annex K.2 procedure), binary
-// PPM and PFM. Replaces the stb_image_write / tinyexr calls of Export.h:14-151 (tinyexr's
-// compressors are not written here).
+// PPM and PFM. Replaces the stb_image_write / tinyexr calls of Export.h:14-151 (of tinyexr's
+// compressors only ZIP is written here). Deflate is this file's own: one block with the fixed
+// Huffman codes of RFC 1951 and hash-chain LZ77 matches.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -71,6 +73,124 @@ void exr_attr(std::vector<uint8_t>& v, const char* name, const char* type, const
     v.insert(v.end(), type, type + std::strlen(type) + 1);
     put_le(v, value.size(), 4);
     v.insert(v.end(), value.begin(), value.end());
+}
+
+// ---------------------------------------------------------------- zlib / deflate (RFC 1950/1951)
+// One deflate block with the fixed Huffman codes of RFC 1951 section 3.2.6 and LZ77 matches
+// found through hash chains over 3-byte prefixes (32 KiB window, at most 64 candidates).
+const uint16_t kLenBase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                               31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+const uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,   25,   33,   49,   65,    97,    129,
+                                193, 257, 385, 513, 769, 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+struct LsbWriter   // deflate packs bits from the least significant end
+{
+    std::vector<uint8_t>& out;
+    uint64_t acc = 0;
+    int n = 0;
+    void bits(uint32_t v, int len)
+    {
+        acc |= (uint64_t)v << n;
+        n += len;
+        while (n >= 8)
+        {
+            out.push_back((uint8_t)acc);
+            acc >>= 8;
+            n -= 8;
+        }
+    }
+    void code(uint32_t c, int len)   // Huffman codes go most significant bit first
+    {
+        uint32_t r = 0;
+        for (int i = 0; i < len; ++i) r |= ((c >> i) & 1u) << (len - 1 - i);
+        bits(r, len);
+    }
+    void flush()
+    {
+        if (n) out.push_back((uint8_t)acc);
+        acc = 0;
+        n = 0;
+    }
+};
+
+void fixed_symbol(LsbWriter& w, int sym)
+{
+    if (sym < 144) w.code(0x30 + sym, 8);
+    else if (sym < 256) w.code(0x190 + (sym - 144), 9);
+    else if (sym < 280) w.code(sym - 256, 7);
+    else w.code(0xC0 + (sym - 280), 8);
+}
+
+std::vector<uint8_t> zlib_compress(const std::vector<uint8_t>& in)
+{
+    std::vector<uint8_t> out{0x78, 0x01};
+    LsbWriter w{out};
+    w.bits(1, 1);   // final block
+    w.bits(1, 2);   // fixed Huffman codes
+    const int kWindow = 32768, kHash = 1 << 15, kChain = 64;
+    std::vector<int> head(kHash, -1), prev(kWindow, -1);
+    auto hash3 = [&](size_t i) { return ((in[i] << 10) ^ (in[i + 1] << 5) ^ in[i + 2]) & (kHash - 1); };
+    auto insert = [&](size_t i) {
+        if (i + 2 >= in.size()) return;
+        const int h = hash3(i);
+        prev[i & (kWindow - 1)] = head[h];
+        head[h] = (int)i;
+    };
+    size_t i = 0;
+    while (i < in.size())
+    {
+        int bestLen = 0, bestDist = 0;
+        if (i + 2 < in.size())
+        {
+            int cand = head[hash3(i)];
+            for (int k = 0; k < kChain && cand >= 0 && (int)i - cand <= kWindow - 1; ++k)
+            {
+                const size_t maxLen = std::min<size_t>(258, in.size() - i);
+                size_t l = 0;
+                while (l < maxLen && in[cand + l] == in[i + l]) ++l;
+                if ((int)l > bestLen)
+                {
+                    bestLen = (int)l;
+                    bestDist = (int)i - cand;
+                    if (l == maxLen) break;
+                }
+                const int nxt = prev[cand & (kWindow - 1)];
+                if (nxt >= cand) break;   // the chain slot was reused by a newer position
+                cand = nxt;
+            }
+        }
+        if (bestLen >= 3)
+        {
+            int lc = 28;
+            while (kLenBase[lc] > bestLen) --lc;
+            fixed_symbol(w, 257 + lc);
+            w.bits((uint32_t)(bestLen - kLenBase[lc]), kLenExtra[lc]);
+            int dc = 29;
+            while (kDistBase[dc] > bestDist) --dc;
+            w.code((uint32_t)dc, 5);
+            w.bits((uint32_t)(bestDist - kDistBase[dc]), kDistExtra[dc]);
+            for (int k = 0; k < bestLen; ++k) insert(i + k);
+            i += bestLen;
+        }
+        else
+        {
+            fixed_symbol(w, in[i]);
+            insert(i);
+            ++i;
+        }
+    }
+    fixed_symbol(w, 256);   // end of block
+    w.flush();
+    uint32_t a = 1, b = 0;
+    for (uint8_t c : in)
+    {
+        a = (a + c) % 65521;
+        b = (b + a) % 65521;
+    }
+    put32(out, (b << 16) | a);
+    return out;
 }
 
 // ---------------------------------------------------------------- baseline JPEG (ITU-T T.81)
@@ -227,37 +347,44 @@ extern "C" {
 lf_status lf_write_png(const char* path, const uint8_t* rgb8, int32_t w, int32_t h)
 {
     if (!path || !rgb8 || w <= 0 || h <= 0) return LF_ERR_INVALID;
-    // raw scanlines, top row first, filter type 0
+    // scanlines top row first, each with the filter (none, sub, up, average, Paeth; PNG
+    // specification section 9) whose output has the smallest sum of absolute signed values
+    const size_t n = (size_t)w * 3;
     std::vector<uint8_t> raw;
-    raw.reserve((size_t)h * (1 + (size_t)w * 3));
+    raw.reserve((size_t)h * (1 + n));
+    std::vector<uint8_t> zero(n, 0), cand[5];
+    for (auto& c : cand) c.resize(n);
     for (int y = h - 1; y >= 0; --y)
     {
-        raw.push_back(0);
-        const uint8_t* row = rgb8 + (size_t)y * w * 3;
-        raw.insert(raw.end(), row, row + (size_t)w * 3);
+        const uint8_t* row = rgb8 + (size_t)y * n;
+        const uint8_t* up = y + 1 < h ? rgb8 + (size_t)(y + 1) * n : zero.data();
+        for (size_t i = 0; i < n; ++i)
+        {
+            const int x = row[i], a = i >= 3 ? row[i - 3] : 0, b = up[i], c = i >= 3 ? up[i - 3] : 0;
+            const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+            const int paeth = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+            cand[0][i] = (uint8_t)x;
+            cand[1][i] = (uint8_t)(x - a);
+            cand[2][i] = (uint8_t)(x - b);
+            cand[3][i] = (uint8_t)(x - ((a + b) >> 1));
+            cand[4][i] = (uint8_t)(x - paeth);
+        }
+        int best = 0;
+        long long bestSum = -1;
+        for (int f = 0; f < 5; ++f)
+        {
+            long long sum = 0;
+            for (size_t i = 0; i < n; ++i) sum += std::abs((int)(int8_t)cand[f][i]);
+            if (bestSum < 0 || sum < bestSum)
+            {
+                bestSum = sum;
+                best = f;
+            }
+        }
+        raw.push_back((uint8_t)best);
+        raw.insert(raw.end(), cand[best].begin(), cand[best].end());
     }
-    // zlib: header, stored blocks of at most 65535 bytes, Adler-32
-    std::vector<uint8_t> z{0x78, 0x01};
-    size_t pos = 0;
-    do
-    {
-        const size_t len = std::min<size_t>(65535, raw.size() - pos);
-        const bool last = pos + len == raw.size();
-        z.push_back(last ? 1 : 0);
-        z.push_back((uint8_t)(len & 0xff));
-        z.push_back((uint8_t)(len >> 8));
-        z.push_back((uint8_t)(~len & 0xff));
-        z.push_back((uint8_t)((~len >> 8) & 0xff));
-        z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + len);
-        pos += len;
-    } while (pos < raw.size());
-    uint32_t a = 1, b = 0;
-    for (uint8_t c : raw)
-    {
-        a = (a + c) % 65521;
-        b = (b + a) % 65521;
-    }
-    put32(z, (b << 16) | a);
+    const std::vector<uint8_t> z = zlib_compress(raw);
     std::vector<uint8_t> png{0x89, 'P', 'N', 'G', 0x0d, 0x0a, 0x1a, 0x0a};
     std::vector<uint8_t> ihdr;
     put32(ihdr, (uint32_t)w);
@@ -366,7 +493,7 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
     }
     v.push_back(0);
     exr_attr(out, "channels", "chlist", v);
-    exr_attr(out, "compression", "compression", {0});
+    exr_attr(out, "compression", "compression", {3});   // ZIP: 16 scanlines per block
     v.clear();
     for (int32_t k : {0, 0, w - 1, h - 1}) put_le(v, (uint32_t)k, 4);
     exr_attr(out, "dataWindow", "box2i", v);
@@ -383,18 +510,35 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
     put_f32(v, 1.0f);
     exr_attr(out, "screenWindowWidth", "float", v);
     out.push_back(0);
-    // one scanline per block: the offset table, then y, byte count and the B, G and R rows.
+    // blocks of 16 scanlines: the offset table, then per block its first y, byte count and data.
     // Rows go out in the order given (the reference writes the bottom-first GL buffer as is).
-    const size_t rowBytes = (size_t)w * 3 * 4;
+    // A block's data is its rows' B, G and R channels, bytes split into even and odd positions,
+    // differenced (d[i] - d[i-1] + 128) and deflated; when that is not smaller, the raw rows.
+    const int nBlocks = (h + 15) / 16;
     const size_t table = out.size();
-    for (int y = 0; y < h; ++y) put_le(out, table + (size_t)h * 8 + (size_t)y * (8 + rowBytes), 8);
-    for (int y = 0; y < h; ++y)
+    out.resize(table + (size_t)nBlocks * 8);
+    std::vector<uint8_t> raw, mixed;
+    for (int blk = 0; blk < nBlocks; ++blk)
     {
-        put_le(out, (uint32_t)y, 4);
-        put_le(out, rowBytes, 4);
-        const float* row = rgbf + (size_t)y * w * 3;
-        for (int c = 2; c >= 0; --c)
-            for (int x = 0; x < w; ++x) put_f32(out, row[x * 3 + c]);
+        const int y0 = blk * 16, y1 = std::min(h, y0 + 16);
+        raw.clear();
+        for (int y = y0; y < y1; ++y)
+        {
+            const float* row = rgbf + (size_t)y * w * 3;
+            for (int c = 2; c >= 0; --c)
+                for (int x = 0; x < w; ++x) put_f32(raw, row[x * 3 + c]);
+        }
+        mixed.resize(raw.size());
+        const size_t half = (raw.size() + 1) / 2;
+        for (size_t k = 0; k < raw.size(); ++k) mixed[(k & 1) ? half + k / 2 : k / 2] = raw[k];
+        for (size_t k = mixed.size() - 1; k > 0; --k) mixed[k] = (uint8_t)(mixed[k] - mixed[k - 1] + 128);
+        const std::vector<uint8_t> z = zlib_compress(mixed);
+        const std::vector<uint8_t>& data = z.size() < raw.size() ? z : raw;
+        const size_t at = out.size();
+        for (int k = 0; k < 8; ++k) out[table + (size_t)blk * 8 + k] = (uint8_t)((uint64_t)at >> (8 * k));
+        put_le(out, (uint32_t)y0, 4);
+        put_le(out, data.size(), 4);
+        out.insert(out.end(), data.begin(), data.end());
     }
     return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
 }

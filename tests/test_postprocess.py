@@ -104,8 +104,29 @@ def read_png(path):
             idat += body
         pos += 12 + n
     raw = zlib.decompress(idat)
-    rows = [raw[y * (3 * w + 1) + 1:(y + 1) * (3 * w + 1)] for y in range(h)]
-    return np.frombuffer(b"".join(rows), np.uint8).reshape(h, w, 3)
+    n = 3 * w
+    out = np.zeros((h, n), np.int64)
+    for y in range(h):   # undo the row filters (PNG specification section 9)
+        f = raw[y * (n + 1)]
+        line = np.frombuffer(raw[y * (n + 1) + 1:(y + 1) * (n + 1)], np.uint8).astype(np.int64)
+        up = out[y - 1] if y else np.zeros(n, np.int64)
+        for i in range(n):
+            a = out[y, i - 3] if i >= 3 else 0
+            b, c = up[i], (up[i - 3] if i >= 3 else 0)
+            if f == 0:
+                pred = 0
+            elif f == 1:
+                pred = a
+            elif f == 2:
+                pred = b
+            elif f == 3:
+                pred = (a + b) // 2
+            else:
+                p = a + b - c
+                pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+            out[y, i] = (line[i] + pred) % 256
+    return out.astype(np.uint8).reshape(h, w, 3)
 
 
 def test_png_and_pfm_writers_round_trip(tmp_path):
@@ -156,7 +177,8 @@ def read_tga(path):
 
 
 def read_exr(path):
-    """Single-part scanline OpenEXR reader for uncompressed 32-bit float channels."""
+    """Single-part scanline OpenEXR reader for 32-bit float channels, uncompressed or ZIP
+    (16-line blocks: zlib, then the byte predictor and the even/odd split undone)."""
     data = open(path, "rb").read()
     assert data[:4] == bytes([0x76, 0x2F, 0x31, 0x01]) and data[4] == 2
     pos, attrs = 8, {}
@@ -168,7 +190,9 @@ def read_exr(path):
                                                 data[type_end + 5:type_end + 5 + size])
         pos = type_end + 5 + size
     pos += 1
-    assert attrs["compression"] == ("compression", b"\0")
+    comp = attrs["compression"][1][0]
+    assert comp in (0, 3)
+    lines = 16 if comp == 3 else 1
     ch, chans = attrs["channels"][1], []
     i = 0
     while ch[i] != 0:
@@ -179,14 +203,43 @@ def read_exr(path):
         i = e + 17
     x0, y0, x1, y1 = struct.unpack("<iiii", attrs["dataWindow"][1])
     w, h = x1 - x0 + 1, y1 - y0 + 1
-    offsets = struct.unpack(f"<{h}Q", data[pos:pos + 8 * h])
+    nblocks = (h + lines - 1) // lines
+    offsets = struct.unpack(f"<{nblocks}Q", data[pos:pos + 8 * nblocks])
     img = np.zeros((h, w, len(chans)), np.float32)
     for off in offsets:
         y, n = struct.unpack("<ii", data[off:off + 8])
-        assert n == 4 * w * len(chans)
-        row = np.frombuffer(data[off + 8:off + 8 + n], "<f4").reshape(len(chans), w)
-        img[y - y0] = row.T
+        rows = min(lines, y0 + h - y)
+        size = 4 * w * len(chans) * rows
+        blk = data[off + 8:off + 8 + n]
+        if n < size:
+            t = np.frombuffer(zlib.decompress(blk), np.uint8).astype(np.int64)
+            t = (np.cumsum(t - 128) + 128) % 256    # t[i] = t[i-1] + d[i] - 128, t[0] = d[0]
+            half = (size + 1) // 2
+            raw = np.empty(size, np.uint8)
+            raw[0::2], raw[1::2] = t[:half], t[half:]
+            blk = raw.tobytes()
+        assert len(blk) == size
+        block = np.frombuffer(blk, "<f4").reshape(rows, len(chans), w)
+        img[y - y0:y - y0 + rows] = block.transpose(0, 2, 1)
     return chans, img
+
+
+def test_png_and_exr_are_deflated(tmp_path):
+    # the writers' own deflate (fixed Huffman codes, LZ77) must round-trip through zlib and
+    # shrink smooth images; noise may stay near its raw size
+    yy, xx = np.mgrid[0:200, 0:300]
+    smooth = np.stack([xx % 256, yy % 256, (xx // 8 + yy // 8) % 256], -1).astype(np.uint8)
+    lf.write_image(tmp_path / "s.png", smooth)
+    assert np.array_equal(read_png(tmp_path / "s.png"), smooth[::-1])
+    assert (tmp_path / "s.png").stat().st_size < smooth.nbytes / 4
+    imgf = (smooth / 255.0).astype(np.float32)
+    lf.write_image(tmp_path / "s.exr", imgf)
+    chans, back = read_exr(tmp_path / "s.exr")
+    assert back[:, :, ::-1].tobytes() == imgf.tobytes()
+    assert (tmp_path / "s.exr").stat().st_size < imgf.nbytes / 2
+    noise = np.random.default_rng(7).integers(0, 256, (64, 65, 3), dtype=np.uint8)
+    lf.write_image(tmp_path / "n.png", noise)
+    assert np.array_equal(read_png(tmp_path / "n.png"), noise[::-1])
 
 
 def test_bmp_tga_exr_writers_round_trip(tmp_path):
