@@ -314,6 +314,10 @@ lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t width, int
 lf_status lf_write_ppm(const char* path, const uint8_t* rgb8, int32_t width, int32_t height);
 lf_status lf_write_pfm(const char* path, const float* rgbf, int32_t width, int32_t height);
 lf_status lf_write_exr(const char* path, const float* rgbf, int32_t width, int32_t height);
+/* EXR with a chosen compression: 0 none, 1 RLE, 2 ZIPS (one-line ZIP blocks), 3 ZIP (the
+ * default of lf_write_exr); PIZ and ZFP are not written. */
+lf_status lf_write_exr_compressed(const char* path, const float* rgbf, int32_t width, int32_t height,
+                                  int32_t compression);
 /* Baseline JPEG (SaveFrameJPG, Export.h:37-46): `quality` 1..100 scales the quantisation
  * tables; 4:4:4 YCbCr; Huffman tables built for the image. Shown upright like PNG. */
 lf_status lf_write_jpg(const char* path, const uint8_t* rgb8, int32_t width, int32_t height, int32_t quality);

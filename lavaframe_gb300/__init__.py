@@ -104,6 +104,7 @@ _SIG = {
     "lf_write_tga": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "lf_write_exr": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32]),
     "lf_write_jpg": (C.c_int, [C.c_char_p, _P, C.c_int32, C.c_int32, C.c_int32]),
+    "lf_write_exr_compressed": (C.c_int, [C.c_char_p, _F, C.c_int32, C.c_int32, C.c_int32]),
     "lf_server_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
     "lf_server_remove_scene": (C.c_int, [_P, C.c_int64]),
@@ -443,16 +444,19 @@ class PostParams(C.Structure):
         return cls(tonemap, 0, 0, 0, 0, 0.05, 5.0, -0.5, 0.5, 0.0, 1.0)
 
 
-def write_image(path, img, jpg_quality=90):
+def write_image(path, img, jpg_quality=90, exr_compression=3):
     """PNG / BMP / TGA / JPEG / PPM from (H, W, 3) uint8, PFM / EXR from float32, chosen by the
-    file extension (PNG otherwise); row 0 = bottom."""
+    file extension (PNG otherwise); row 0 = bottom. EXR compression: 0 none, 1 RLE, 2 ZIPS,
+    3 ZIP."""
     path = str(path)
     h, w = img.shape[:2]
     ext = path.rsplit(".", 1)[-1].lower()
     if ext in ("pfm", "exr"):
         a = np.ascontiguousarray(img, np.float32)
-        fn = lib().lf_write_exr if ext == "exr" else lib().lf_write_pfm
-        _chk(fn(path.encode(), _fp(a), w, h))
+        if ext == "exr":
+            _chk(lib().lf_write_exr_compressed(path.encode(), _fp(a), w, h, int(exr_compression)))
+        else:
+            _chk(lib().lf_write_pfm(path.encode(), _fp(a), w, h))
     else:
         a = np.ascontiguousarray(img, np.uint8)
         if ext in ("jpg", "jpeg"):

@@ -1,10 +1,10 @@
 // Image export: PNG (row filters chosen per row, deflated; CRC-32 and Adler-32 per the PNG and
 // zlib specifications), BMP (24-bit, uncompressed), TGA (run-length encoded true colour, the
 // form stb_image_write writes by default), OpenEXR (single-part scanline, 32-bit float B, G, R
-// channels, ZIP compression as the reference's default), baseline JPEG (ITU-T T.81: 4:4:4 YCbCr, quality-scaled Annex K
+// channels; none, RLE, ZIPS or ZIP compression, ZIP by default as in the reference), baseline JPEG (ITU-T T.81: 4:4:4 YCbCr, quality-scaled Annex K
 // quantisation tables, Huffman tables built for each image by the Annex K.2 procedure), binary
-// PPM and PFM. Replaces the stb_image_write / tinyexr calls of Export.h:14-151 (of tinyexr's
-// compressors only ZIP is written here). Deflate is this file's own: one block with the fixed
+// PPM and PFM. Replaces the stb_image_write / tinyexr calls of Export.h:14-151 (tinyexr's PIZ
+// and ZFP compressors are not written here). Deflate is this file's own: one block with the fixed
 // Huffman codes of RFC 1951 and hash-chain LZ77 matches.
 #include <algorithm>
 #include <cmath>
@@ -190,6 +190,34 @@ std::vector<uint8_t> zlib_compress(const std::vector<uint8_t>& in)
         b = (b + a) % 65521;
     }
     put32(out, (b << 16) | a);
+    return out;
+}
+
+// OpenEXR's run-length code: a run of 3 to 128 equal bytes is (count - 1, byte); other bytes go
+// in literal groups of up to 128 as (-count, bytes...).
+std::vector<uint8_t> rle_compress(const std::vector<uint8_t>& in)
+{
+    std::vector<uint8_t> out;
+    size_t i = 0;
+    while (i < in.size())
+    {
+        size_t run = 1;
+        while (i + run < in.size() && run < 128 && in[i + run] == in[i]) ++run;
+        if (run >= 3)
+        {
+            out.push_back((uint8_t)(run - 1));
+            out.push_back(in[i]);
+            i += run;
+            continue;
+        }
+        size_t lit = 0;   // up to the next run of three
+        while (i + lit < in.size() && lit < 128 &&
+               !(i + lit + 2 < in.size() && in[i + lit] == in[i + lit + 1] && in[i + lit] == in[i + lit + 2]))
+            ++lit;
+        out.push_back((uint8_t)(-(int)lit));
+        out.insert(out.end(), in.begin() + (long)i, in.begin() + (long)(i + lit));
+        i += lit;
+    }
     return out;
 }
 
@@ -477,9 +505,9 @@ lf_status lf_write_tga(const char* path, const uint8_t* rgb8, int32_t w, int32_t
     return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
 }
 
-lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h)
+lf_status lf_write_exr_compressed(const char* path, const float* rgbf, int32_t w, int32_t h, int32_t compression)
 {
-    if (!path || !rgbf || w <= 0 || h <= 0) return LF_ERR_INVALID;
+    if (!path || !rgbf || w <= 0 || h <= 0 || compression < 0 || compression > 3) return LF_ERR_INVALID;
     std::vector<uint8_t> out{0x76, 0x2f, 0x31, 0x01, 2, 0, 0, 0};   // magic, version 2, scanline
     std::vector<uint8_t> v;
     for (const char* c : {"B", "G", "R"})   // channel list in name order, 32-bit float, 1x1 sampling
@@ -493,7 +521,8 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
     }
     v.push_back(0);
     exr_attr(out, "channels", "chlist", v);
-    exr_attr(out, "compression", "compression", {3});   // ZIP: 16 scanlines per block
+    // 0 none and 1 RLE (one scanline per block), 2 ZIPS (one), 3 ZIP (16)
+    exr_attr(out, "compression", "compression", {(uint8_t)compression});
     v.clear();
     for (int32_t k : {0, 0, w - 1, h - 1}) put_le(v, (uint32_t)k, 4);
     exr_attr(out, "dataWindow", "box2i", v);
@@ -510,17 +539,19 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
     put_f32(v, 1.0f);
     exr_attr(out, "screenWindowWidth", "float", v);
     out.push_back(0);
-    // blocks of 16 scanlines: the offset table, then per block its first y, byte count and data.
+    // blocks of scanlines: the offset table, then per block its first y, byte count and data.
     // Rows go out in the order given (the reference writes the bottom-first GL buffer as is).
-    // A block's data is its rows' B, G and R channels, bytes split into even and odd positions,
-    // differenced (d[i] - d[i-1] + 128) and deflated; when that is not smaller, the raw rows.
-    const int nBlocks = (h + 15) / 16;
+    // A block's data is its rows' B, G and R channels; RLE and ZIP split the bytes into even and
+    // odd positions and difference them (d[i] - d[i-1] + 128), then run-length code or deflate
+    // them; when that is not smaller, the raw rows are stored.
+    const int lines = compression == 3 ? 16 : 1;
+    const int nBlocks = (h + lines - 1) / lines;
     const size_t table = out.size();
     out.resize(table + (size_t)nBlocks * 8);
     std::vector<uint8_t> raw, mixed;
     for (int blk = 0; blk < nBlocks; ++blk)
     {
-        const int y0 = blk * 16, y1 = std::min(h, y0 + 16);
+        const int y0 = blk * lines, y1 = std::min(h, y0 + lines);
         raw.clear();
         for (int y = y0; y < y1; ++y)
         {
@@ -528,12 +559,16 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
             for (int c = 2; c >= 0; --c)
                 for (int x = 0; x < w; ++x) put_f32(raw, row[x * 3 + c]);
         }
-        mixed.resize(raw.size());
-        const size_t half = (raw.size() + 1) / 2;
-        for (size_t k = 0; k < raw.size(); ++k) mixed[(k & 1) ? half + k / 2 : k / 2] = raw[k];
-        for (size_t k = mixed.size() - 1; k > 0; --k) mixed[k] = (uint8_t)(mixed[k] - mixed[k - 1] + 128);
-        const std::vector<uint8_t> z = zlib_compress(mixed);
-        const std::vector<uint8_t>& data = z.size() < raw.size() ? z : raw;
+        std::vector<uint8_t> z;
+        if (compression > 0)
+        {
+            mixed.resize(raw.size());
+            const size_t half = (raw.size() + 1) / 2;
+            for (size_t k = 0; k < raw.size(); ++k) mixed[(k & 1) ? half + k / 2 : k / 2] = raw[k];
+            for (size_t k = mixed.size() - 1; k > 0; --k) mixed[k] = (uint8_t)(mixed[k] - mixed[k - 1] + 128);
+            z = compression == 1 ? rle_compress(mixed) : zlib_compress(mixed);
+        }
+        const std::vector<uint8_t>& data = compression > 0 && z.size() < raw.size() ? z : raw;
         const size_t at = out.size();
         for (int k = 0; k < 8; ++k) out[table + (size_t)blk * 8 + k] = (uint8_t)((uint64_t)at >> (8 * k));
         put_le(out, (uint32_t)y0, 4);
@@ -541,6 +576,11 @@ lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h
         out.insert(out.end(), data.begin(), data.end());
     }
     return write_file(path, out.data(), out.size()) ? LF_OK : LF_ERR_IO;
+}
+
+lf_status lf_write_exr(const char* path, const float* rgbf, int32_t w, int32_t h)
+{
+    return lf_write_exr_compressed(path, rgbf, w, h, 3);
 }
 
 lf_status lf_write_jpg(const char* path, const uint8_t* rgb8, int32_t w, int32_t h, int32_t quality)

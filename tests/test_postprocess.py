@@ -177,8 +177,8 @@ def read_tga(path):
 
 
 def read_exr(path):
-    """Single-part scanline OpenEXR reader for 32-bit float channels, uncompressed or ZIP
-    (16-line blocks: zlib, then the byte predictor and the even/odd split undone)."""
+    """Single-part scanline OpenEXR reader for 32-bit float channels: uncompressed, RLE, ZIPS or
+    ZIP (run-length or zlib decoding, then the byte predictor and the even/odd split undone)."""
     data = open(path, "rb").read()
     assert data[:4] == bytes([0x76, 0x2F, 0x31, 0x01]) and data[4] == 2
     pos, attrs = 8, {}
@@ -191,7 +191,7 @@ def read_exr(path):
         pos = type_end + 5 + size
     pos += 1
     comp = attrs["compression"][1][0]
-    assert comp in (0, 3)
+    assert comp in (0, 1, 2, 3)
     lines = 16 if comp == 3 else 1
     ch, chans = attrs["channels"][1], []
     i = 0
@@ -212,7 +212,20 @@ def read_exr(path):
         size = 4 * w * len(chans) * rows
         blk = data[off + 8:off + 8 + n]
         if n < size:
-            t = np.frombuffer(zlib.decompress(blk), np.uint8).astype(np.int64)
+            if comp == 1:
+                dec, k = bytearray(), 0
+                while k < len(blk):
+                    c = struct.unpack("b", blk[k:k + 1])[0]
+                    if c < 0:
+                        dec += blk[k + 1:k + 1 - c]
+                        k += 1 - c
+                    else:
+                        dec += blk[k + 1:k + 2] * (c + 1)
+                        k += 2
+                blk = bytes(dec)
+            else:
+                blk = zlib.decompress(blk)
+            t = np.frombuffer(blk, np.uint8).astype(np.int64)
             t = (np.cumsum(t - 128) + 128) % 256    # t[i] = t[i-1] + d[i] - 128, t[0] = d[0]
             half = (size + 1) // 2
             raw = np.empty(size, np.uint8)
@@ -237,6 +250,17 @@ def test_png_and_exr_are_deflated(tmp_path):
     chans, back = read_exr(tmp_path / "s.exr")
     assert back[:, :, ::-1].tobytes() == imgf.tobytes()
     assert (tmp_path / "s.exr").stat().st_size < imgf.nbytes / 2
+    for comp in (0, 1, 2, 3):   # none, RLE, ZIPS, ZIP
+        lf.write_image(tmp_path / f"c{comp}.exr", imgf, exr_compression=comp)
+        _, back = read_exr(tmp_path / f"c{comp}.exr")
+        assert back[:, :, ::-1].tobytes() == imgf.tobytes(), comp
+    # long runs for the run-length code (a constant like 0.25 leaves the predictor's odd-byte
+    # half alternating, which run-length coding cannot shorten)
+    flat = np.zeros((40, 50, 3), np.float32)
+    flat[5:9, 10:20] = 1.0
+    lf.write_image(tmp_path / "f.exr", flat, exr_compression=1)
+    assert read_exr(tmp_path / "f.exr")[1].tobytes() == flat.tobytes()
+    assert (tmp_path / "f.exr").stat().st_size < flat.nbytes / 10
     noise = np.random.default_rng(7).integers(0, 256, (64, 65, 3), dtype=np.uint8)
     lf.write_image(tmp_path / "n.png", noise)
     assert np.array_equal(read_png(tmp_path / "n.png"), noise[::-1])
