@@ -323,17 +323,21 @@ lf_status lf_write_exr_compressed(const char* path, const float* rgbf, int32_t w
 lf_status lf_write_jpg(const char* path, const uint8_t* rgb8, int32_t width, int32_t height, int32_t quality);
 
 /* Render without allocating (no counterpart in the reference). For callers that cannot
- * allocate device memory while rendering - plugin hosts that hand out a fixed arena,
- * frame loops that forbid allocation, work recorded into CUDA graphs. Accumulates samples
- * [first_sample, first_sample + count) of `p` into the caller's device buffer `d_accum`
- * (width*height float4 RGBA32F, row 0 = bottom, A unused; zero it before the first call),
- * in sample order, with the same results as lf_frame_render.
- * All wavefront state lives in one fixed device array of the library (about 31.5 MiB per
- * GPU that loads it, held until exit): one tile (tile_width x tile_height, or the whole
- * frame) may have at most 131072 pixels, larger tiles are rejected with LF_ERR_INVALID.
+ * allocate device memory while they render: plugin hosts that give the renderer a fixed
+ * device arena and account for every byte on the GPU themselves, and real-time frame loops
+ * that forbid allocation inside a frame (cudaMalloc/cudaFree can synchronise the device and
+ * stall the frame, and can fail once another allocator holds the memory). Accumulates
+ * samples [first_sample, first_sample + count) of `p` into the caller's device buffer
+ * `d_accum` (width*height float4 RGBA32F, row 0 = bottom, A unused; zero it before the first
+ * call), in sample order; the sums are bit-identical to lf_frame_render's.
+ * All wavefront state lives in one fixed device array of the library (30 MiB + 256 B, i.e.
+ * 31.5 MB, on every GPU that loads it, held until exit): one tile (tile_width x tile_height,
+ * or the whole frame) may have at most 131072 pixels, larger tiles are rejected with
+ * LF_ERR_INVALID. The call makes no cudaMalloc/cudaFree and no allocating library call.
  * The first call on a device resolves the array's address (cudaGetSymbolAddress); make it
- * before any stream capture. Every call reuses the same array: calls that overlap on the
- * GPU (other threads, other contexts on the same device) race. Synchronous. */
+ * before any stream capture. Every call reuses the same array and clears the queue sizes,
+ * status word and counters it keeps at the start: calls that overlap on the GPU (other
+ * threads, other contexts on the same device) race. Returns after the GPU has finished. */
 lf_status lf_render_noalloc(lf_scene* sc, const lf_render_params* p, int32_t first_sample, int32_t count,
                             void* d_accum);
 

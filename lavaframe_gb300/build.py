@@ -96,7 +96,7 @@ def build_oracle(verbose: bool = False, force: bool = False) -> Path:
 
 def build_reference(verbose: bool = False, force: bool = False):
     """Compiles the reference's own host code and shaders into oracle/_ref when a reference
-    checkout is available (LAVAFRAME_REFERENCE or the default location)."""
+    checkout is available (LAVAFRAME_REFERENCE, else a `reference` directory beside the repository)."""
     script = ORACLE / "build_ref.py"
     if not script.exists():
         return None

@@ -1648,10 +1648,11 @@ lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes)
 
 // ------------------------------------------------------------------ render without allocating
 // Some callers cannot allocate device memory at render time: plugin hosts that hand the
-// renderer a fixed device arena, real-time loops that forbid allocation inside a frame, and
-// code that records work into a CUDA graph (cudaMalloc is not allowed while a stream is being
-// captured). lf_render_noalloc serves them: all wavefront state lives in one file-scope
-// device array of fixed size, and the accumulation buffer is the caller's.
+// renderer a fixed device arena and account for every byte on the GPU themselves, and
+// real-time loops that forbid allocation inside a frame (cudaMalloc and cudaFree can
+// synchronise the device and stall the frame, and may fail once another allocator holds the
+// memory). lf_render_noalloc serves them: all wavefront state lives in one file-scope device
+// array of fixed size, and the accumulation buffer is the caller's.
 namespace
 {
 constexpr long long kNoAllocPaths = 131072;   // path slots = max pixels of one tile
@@ -1664,7 +1665,8 @@ constexpr size_t kNoAllocBytes = kNoAllocHeader + 8 * noalloc_round(kNoAllocPath
                                  noalloc_round(kNoAllocPaths * sizeof(ShadowRec));
 }
 
-// About 31.5 MiB on every GPU that loads the library, kept until the process exits.
+// 30 MiB + 256 B (31.5 MB) on every GPU that loads the library, kept until the process exits.
+static_assert(kNoAllocBytes == 30ull * 1024 * 1024 + 256, "documented size of the no-alloc scratch array");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace

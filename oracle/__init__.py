@@ -23,7 +23,7 @@ def lib():
             raise RuntimeError(f"{LIB} missing; build with lavaframe_gb300.build.build_oracle()")
         L = C.CDLL(str(LIB))
         P = C.c_void_p
-        L.lfo_trace_closest.argtypes = [P, P, C.c_int64, P, C.c_int32, C.c_float, C.c_float, C.c_int32, P]
+        L.lfo_trace_closest.argtypes = [P, P, C.c_int64, P, C.c_int32, C.c_float, C.c_float, C.c_int32, P, P]
         L.lfo_trace_any.argtypes = [P, P, C.c_int64, P, C.c_int32, C.c_float, C.c_float, C.c_int32, P]
         L.lfo_render.argtypes = [P, P, C.c_int32, C.c_int32, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_float,
                                  C.c_float, P]
@@ -99,14 +99,17 @@ def rand_sequence(px, py, frame, n, seed=0):
 HIT_DTYPE = np.dtype([("t", "<f4"), ("instance", "<i4"), ("prim", "<i4"), ("light", "<i4")])
 
 
-def trace_closest(view, rays, lights=False, cull_rel=-1.0, cull_abs=0.0, threads=0):
-    """Hits (t, instance, packed triangle, light) per ray; cull_rel < 0 = shader semantics."""
+def trace_closest(view, rays, lights=False, cull_rel=-1.0, cull_abs=0.0, threads=0, want_ties=False):
+    """Hits (t, instance, packed triangle, light) per ray; cull_rel < 0 = shader semantics.
+    With want_ties, also a per-ray flag: 1 where the closest triangle hit has an
+    equal-distance competitor (the answer then depends only on the visit order)."""
     rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
     hits = np.empty(len(rays), HIT_DTYPE)
     stats = np.zeros(5, np.uint64)
+    ties = np.zeros(len(rays), np.uint8) if want_ties else None
     lib().lfo_trace_closest(C.addressof(view), rays.ctypes.data, len(rays), hits.ctypes.data, int(lights), cull_rel,
-                            cull_abs, threads, stats.ctypes.data)
-    return hits, stats
+                            cull_abs, threads, stats.ctypes.data, ties.ctypes.data if want_ties else None)
+    return (hits, stats, ties) if want_ties else (hits, stats)
 
 
 def trace_any(view, rays, lights=False, cull_rel=-1.0, cull_abs=0.0, threads=0):

@@ -23,7 +23,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF = Path(os.environ.get("LAVAFRAME_REFERENCE", "/root/reference"))
+# the reference checkout: LAVAFRAME_REFERENCE, else a `reference` directory beside this repository
+REF = Path(os.environ.get("LAVAFRAME_REFERENCE", HERE.parent.parent / "reference"))
 
 
 def _run(cmd):

@@ -163,6 +163,7 @@ struct HitRec
     v3 bary;
     v3 fhp;
     v3 tempTex;
+    float tieT = -1.0f;   // distance of the last candidate rejected for t == tBest (test diagnostics only)
 };
 
 // Two-level traversal shared by ClosestHit (closest_hit.glsl:69-201) and AnyHit
@@ -215,7 +216,9 @@ bool Traverse(const Prepared& P, const Options& O, v3 ro0, v3 rd0, float& t, boo
                 float uy = lfc::dot(r_d, qv) / det;
                 float uz = lfc::dot(e1, qv) / det;
                 float uw = 1.0f - ux - uy;
-                if (ux >= 0.f && uy >= 0.f && uz >= 0.f && uw >= 0.f && uz < t)
+                const bool inside = ux >= 0.f && uy >= 0.f && uz >= 0.f && uw >= 0.f;
+                if (!any && inside && uz == t) h->tieT = uz;   // equal-distance competitor (strict < keeps the first)
+                if (inside && uz < t)
                 {
                     if (any)
                     {
@@ -1151,9 +1154,11 @@ static View to_view(const lfo_view* s)
 
 // Closest hit for n rays (8 floats each). hits: 4 x int32 per ray (t bits, instance,
 // packed triangle, light). stats (optional): node visits, triangle tests, leaf visits,
-// stack overflows. cull_rel < 0 reproduces the shader (no culling).
+// stack overflows. cull_rel < 0 reproduces the shader (no culling). ties (optional): 1 for a
+// ray whose closest triangle hit has an equal-distance competitor (a grazing edge or vertex,
+// or coincident geometry), where only the visit order decides the answer.
 int lfo_trace_closest(const lfo_view* sv, const float* rays, int64_t n, int32_t* hits, int32_t lights, float cull_rel,
-                      float cull_abs, int32_t threads, uint64_t* stats)
+                      float cull_abs, int32_t threads, uint64_t* stats, uint8_t* ties)
 {
     Prepared P;
     prepare(to_view(sv), P);
@@ -1180,6 +1185,7 @@ int lfo_trace_closest(const lfo_view* sv, const float* rays, int64_t n, int32_t*
             o[1] = tri ? st.inst : -1;
             o[2] = tri ? st.triPacked : -1;
             o[3] = st.isEmitter ? st.light : -1;
+            if (ties) ties[i] = (tri && st.tieT == t) ? 1 : 0;
         }
     });
     if (stats)

@@ -25,7 +25,8 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("LAVAFRAME_REFERENCE", "/root/reference"))
+# the reference checkout: LAVAFRAME_REFERENCE, else a `reference` directory beside this repository
+REF = Path(os.environ.get("LAVAFRAME_REFERENCE", HERE.parent.parent / "reference"))
 SHADERS = REF / "shaders"
 CSRC = HERE.parent / "lavaframe_gb300" / "csrc"
 

@@ -7,7 +7,8 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 
-REFERENCE = Path(os.environ.get("LAVAFRAME_REFERENCE", "/root/reference"))
+# the reference checkout: LAVAFRAME_REFERENCE, else a `reference` directory beside this repository
+REFERENCE = Path(os.environ.get("LAVAFRAME_REFERENCE", ROOT.parent / "reference"))
 REF_REF = ROOT / "oracle" / "_ref"
 
 

@@ -1,0 +1,147 @@
+"""CUDA path vs the CPU oracle at the workloads' full sizes, through the C ABI.
+
+The other parity tests use reduced scenes; these run the configurations the throughput
+figures are quoted on and compare every value the oracle produces for them:
+
+  C1  procedural Cornell box, 256x256, 64 spp, depth 4: every path and the accumulation buffer
+  C2  10,485,760-triangle soup (2^20 instances x 10), all 2^24 rays: closest-hit instance,
+      triangle and t bit for bit (checked in chunks), any-hit answers; rays whose closest hit
+      has an equal-distance competitor (grazing edges / vertices) are counted by the oracle
+  C3  13 icospheres (1,064,960 triangles) with the HDR environment, 1920x1080, 16 spp, depth 8,
+      every 4th pixel row; and the 64-icosphere 5,242,880-triangle scene, every 16th row
+  C4  occluded-light room, 16,700 boxes (~200k triangles), 1280x720, depth 10, 4 spp, every
+      4th pixel row
+
+Bars: hit ids and t bit-exact; per-path radiance bit-exact, with the 1e-4 relative tolerance
+as the reported fallback bar. When LF_PARITY_REPORT names a file, the counts are appended to it
+as JSON lines.
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+import lavaframe_gb300 as lf
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+PATH_RTOL = 1e-4
+
+
+def report(name, **kw):
+    kw["case"] = name
+    line = json.dumps(kw)
+    print(line)
+    path = os.environ.get("LF_PARITY_REPORT")
+    if path:
+        with open(path, "a") as fh:
+            fh.write(line + "\n")
+
+
+def path_mismatch(dev, ref):
+    """(paths not bit-identical, largest relative difference) over (..., 3) radiance arrays."""
+    exact = (dev.view(np.uint32) == ref.view(np.uint32)).all(axis=-1)
+    both = np.isfinite(dev) & np.isfinite(ref)
+    rel = np.where(both, np.abs(dev - ref) / np.maximum(np.abs(ref), 1e-6), 0.0)
+    return int((~exact).sum()), float(rel.max()) if rel.size else 0.0
+
+
+def render_rows(ctx, s, p, spp, row_stride):
+    """GPU render of the whole frame (one pass of `spp` samples, so every path can be read
+    back) and the oracle on the rows y % row_stride == 0; returns per-path radiance of those
+    rows from both sides and the device accumulation rows."""
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p)
+    f.set_batch(spp)
+    t0 = time.time()
+    f.render(0, spp)
+    f.sync()
+    t_gpu = time.time() - t0
+    dev_paths = f.paths(spp)[:, ::row_stride]
+    dev_acc = f.accum()[::row_stride]
+    f.close()
+    ds.close()
+    t0 = time.time()
+    ref_acc, ref_paths, ctr = oracle.render(s.view(), p, 0, spp, want_paths=True, row_stride=row_stride)
+    t_cpu = time.time() - t0
+    return dev_paths, ref_paths[:, ::row_stride], dev_acc, ref_acc[::row_stride], ctr, t_gpu, t_cpu
+
+
+def test_c1_cornell_full_config(ctx):
+    s = lf.HostScene().gen_cornell(256, 256).build()
+    p = s.render_params()
+    assert (p.width, p.height, p.max_depth) == (256, 256, 4)
+    dev_paths, ref_paths, dev_acc, ref_acc, ctr, t_gpu, t_cpu = render_rows(ctx, s, p, 64, 1)
+    bad, rel = path_mismatch(dev_paths, ref_paths)
+    report("c1_cornell_256x256_64spp_depth4", paths=int(dev_paths.shape[0] * 256 * 256), mismatched_paths=bad,
+           max_rel=rel, accum_identical=dev_acc.tobytes() == ref_acc.tobytes(), oracle_s=t_cpu)
+    assert bad == 0 or rel <= PATH_RTOL
+    assert bad == 0
+    assert dev_acc.tobytes() == ref_acc.tobytes()
+
+
+def test_c2_microbench_all_rays(ctx):
+    s = lf.HostScene().gen_soup(1 << 20, 10, 1).build()
+    view = s.view()
+    assert view.num_tris == 10485760
+    a = s.arrays()
+    root = a["nodes"][a["top_level_index"]]
+    n = 1 << 24
+    rays = lf.gen_rays(root[0:3], root[3:6], n, 2)
+    ds = ctx.upload(s)
+    dev = ctx.trace_closest(ds, rays)
+    occ = ctx.trace_any(ds, rays)
+    ds.close()
+    extent = float(np.abs(root[:6]).max())
+    cull_abs = 64 * float(np.spacing(np.float32(extent)))
+    chunk = 1 << 22
+    bad_ids, tie_ids, bad_any = [], [], 0
+    t0 = time.time()
+    for i in range(0, n, chunk):
+        r = rays[i:i + chunk]
+        ref, _, ties = oracle.trace_closest(view, r, cull_rel=1e-4, cull_abs=cull_abs, want_ties=True)
+        d = dev[i:i + chunk]
+        same = ((d["t"].view(np.uint32) == ref["t"].view(np.uint32)) & (d["instance"] == ref["instance"]) &
+                (d["prim"] == ref["prim"]) & (d["light"] == ref["light"]))
+        bad_ids.extend((i + np.nonzero(~same)[0]).tolist())
+        tie_ids.extend((i + np.nonzero(ties)[0]).tolist())
+        ref_occ, _ = oracle.trace_any(view, r, cull_rel=1e-4, cull_abs=cull_abs)
+        bad_any += int((ref_occ != occ[i:i + chunk]).sum())
+    t_cpu = time.time() - t0
+    report("c2_microbench_2^24_rays", rays=n, hit_fraction=float((dev["prim"] >= 0).mean()),
+           mismatched_closest=len(bad_ids), mismatched_rays=bad_ids[:64], mismatched_any=bad_any,
+           equal_distance_ties=len(tie_ids), tie_rays=tie_ids[:64], tie_fraction=len(tie_ids) / n, oracle_s=t_cpu)
+    assert len(bad_ids) == 0, f"{len(bad_ids)} of {n} closest hits differ: {bad_ids[:16]}"
+    assert bad_any == 0
+    assert len(tie_ids) <= 1e-6 * n
+
+
+@pytest.mark.parametrize("instances,row_stride", [(13, 4), (64, 16)])
+def test_c3_icospheres_full_config(ctx, instances, row_stride):
+    s = lf.HostScene().gen_icospheres(instances, 6, 3, 1024, 512).build()
+    p = s.render_params()
+    assert (p.width, p.height, p.max_depth) == (1920, 1080, 8)
+    dev_paths, ref_paths, dev_acc, ref_acc, ctr, t_gpu, t_cpu = render_rows(ctx, s, p, 16, row_stride)
+    bad, rel = path_mismatch(dev_paths, ref_paths)
+    report(f"c3_{instances}_icospheres_1920x1080_16spp_depth8_rows_every_{row_stride}",
+           triangles=int(s.view().num_tris), paths=int(dev_paths[..., 0].size), mismatched_paths=bad, max_rel=rel,
+           accum_rows_identical=dev_acc.tobytes() == ref_acc.tobytes(), oracle_s=t_cpu)
+    assert bad == 0 or rel <= PATH_RTOL
+    assert dev_acc.tobytes() == ref_acc.tobytes() or bad > 0
+
+
+def test_c4_room_full_config(ctx):
+    s = lf.HostScene().gen_room(16700, 4).build()
+    p = s.render_params()
+    p.width, p.height = 1280, 720
+    assert p.max_depth == 10
+    dev_paths, ref_paths, dev_acc, ref_acc, ctr, t_gpu, t_cpu = render_rows(ctx, s, p, 4, 4)
+    bad, rel = path_mismatch(dev_paths, ref_paths)
+    report("c4_room_16700_boxes_1280x720_4spp_depth10_rows_every_4", triangles=int(s.view().num_tris),
+           paths=int(dev_paths[..., 0].size), mismatched_paths=bad, max_rel=rel,
+           accum_rows_identical=dev_acc.tobytes() == ref_acc.tobytes(), oracle_s=t_cpu)
+    assert bad == 0 or rel <= PATH_RTOL
+    assert dev_acc.tobytes() == ref_acc.tobytes() or bad > 0
