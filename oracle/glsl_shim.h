@@ -219,6 +219,13 @@ inline vec4 clamp(const vec4& x, float lo, float hi)
 {
     return vec4(clamp(x.x, lo, hi), clamp(x.y, lo, hi), clamp(x.z, lo, hi), clamp(x.w, lo, hi));
 }
+inline vec4 max(const vec4& a, const vec4& b) { return vec4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w)); }
+// distance(a, b) = length(a - b): differences, squares and sum in component order, IEEE sqrt
+inline float distance(const vec2& a, const vec2& b)
+{
+    float dx = a.x - b.x, dy = a.y - b.y;
+    return ::sqrtf(dx * dx + dy * dy);
+}
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 inline vec3 mix(const vec3& x, const vec3& y, float a)
 {

@@ -86,6 +86,19 @@ RefScene* ref_scene_build(int nmeshes, const int* counts, const float* verts, co
     return r;
 }
 
+// Scene::RebuildInstances (Scene.cpp:165-178) after new transforms and materials for the
+// first n instances: a fresh TLAS, BvhTranslator::UpdateTLAS over the TLAS part of the node
+// array, transforms copied - the host half of an instance move.
+void ref_scene_move_instances(RefScene* r, int n, const float* xf, const int* mat)
+{
+    for (int i = 0; i < n && i < (int)r->scene->meshInstances.size(); ++i)
+    {
+        std::memcpy(r->scene->meshInstances[i].transform.data, xf + (size_t)i * 16, 64);
+        r->scene->meshInstances[i].materialID = mat[i];
+    }
+    r->scene->RebuildInstances();
+}
+
 void ref_scene_free(RefScene* r)
 {
     if (!r) return;

@@ -12,7 +12,9 @@ constructs C++ spells differently - nothing else:
 Each combination of the preprocessor switches TiledRenderer injects (ENVMAP, LIGHTS, RR with
 RR_DEPTH, CONSTANT_BG; TiledRenderer.cpp:78-91) becomes one C++ struct whose members are the
 shader's uniforms and globals and whose member functions are the shader's functions.
-glsl_shim.h supplies the GLSL types and built-ins. Output goes to oracle/_ref/ only.
+shaders/postprocess.glsl, the display pass, goes through the same rewriting into one more
+struct driven once per output pixel (refsh_postprocess). glsl_shim.h supplies the GLSL types
+and built-ins. Output goes to oracle/_ref/ only.
 """
 from __future__ import annotations
 
@@ -103,6 +105,59 @@ extern "C" int refsh_render(const lfo_view* v, const lfo_params* p, int first, i
 """
 
 
+def post_source(body: str) -> str:
+    """postprocess.glsl as a struct whose members are its uniforms, its in/out variables and its
+    functions, plus a driver that runs main() once per output pixel the way TiledRenderer's
+    display pass does (TiledRenderer.cpp:540-552): TexCoords at the pixel centre, the
+    accumulation texture (RGB32F, GL_LINEAR, GL_REPEAT) bound as pathTraceTexture."""
+    return f"""#include "glsl_shim.h"
+#include <cstdint>
+namespace glsl {{
+struct RefPost {{
+{body}
+}};
+}}
+struct PostIn
+{{
+    int32_t tonemap, use_ca, use_ca_distortion, use_vignette, preview;
+    float ca_distance, ca_p1, ca_p2, ca_p3, vignette_intensity, vignette_power;
+}};
+// rgbf: W x H x 3 colour of the display pass, row 0 at the bottom.
+extern "C" int refsh_postprocess(const float* accum_rgb, int W, int H, const PostIn* q, int samples, float* rgbf)
+{{
+    glsl::RefPost s{{}};
+    s.pathTraceTexture.data = accum_rgb;
+    s.pathTraceTexture.w = W;
+    s.pathTraceTexture.h = H;
+    s.pathTraceTexture.comps = 3;
+    s.pathTraceTexture.linear = true;
+    s.isInPreview = q->preview != 0;
+    s.invSampleCounter = 1.0f / (float)samples;
+    s.tonemapIndex = q->tonemap;
+    s.useCA = q->use_ca != 0;
+    s.useCADistortion = q->use_ca_distortion != 0;
+    s.caDistance = q->ca_distance;
+    s.caP1 = q->ca_p1;
+    s.caP2 = q->ca_p2;
+    s.caP3 = q->ca_p3;
+    s.useVignette = q->use_vignette != 0;
+    s.vignetteIntensity = q->vignette_intensity;
+    s.vignettePower = q->vignette_power;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+        {{
+            s.TexCoords = glsl::vec2(((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H);
+            s.main();
+            float* o = rgbf + ((size_t)y * W + x) * 3;
+            o[0] = s.color.x;
+            o[1] = s.color.y;
+            o[2] = s.color.z;
+        }}
+    return 0;
+}}
+"""
+
+
 def run(cmd):
     r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True)
     if r.returncode != 0:
@@ -133,6 +188,9 @@ def main():
     d = gen / "dispatch.cpp"
     d.write_text(dispatcher())
     srcs.append(d)
+    post = gen / "post.cpp"
+    post.write_text(post_source(to_cpp((SHADERS / "postprocess.glsl").read_text())))
+    srcs.append(post)
     flags = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", HERE, "-I", CSRC]
     objs = [gen / (s.stem + ".o") for s in srcs]
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:

@@ -42,7 +42,7 @@ def build(name):
         s.gen_cornell(32 if name != "cornell_lights" else 24, 32 if name != "cornell_lights" else 24)
     elif name == "room":
         s.gen_room(300, 4)
-    elif name in ("icospheres", "icospheres_constbg_tiled", "icospheres_lens"):
+    elif name in ("icospheres", "icospheres_constbg_tiled", "icospheres_lens", "icospheres_absorb"):
         s.gen_icospheres(6, 3, 5, 64, 32)
     else:
         raise KeyError(name)
@@ -71,6 +71,18 @@ def build(name):
         p.cam_focal_dist = 40.0
         p.hdr_multiplier = 2.0
         p.frame_base = 7
+    if name == "icospheres_absorb":
+        # transmissive, absorbing interiors (pathtrace.glsl:263-272): every material but the
+        # first becomes a smooth dielectric whose extinction is reached at atDistance
+        p.width, p.height = 48, 27
+        m = a["materials"].copy()
+        m[1:, 8] = 0.0                       # metallic
+        m[1:, 9] = 0.05                      # roughness
+        m[1:, 16] = 1.0                      # transmission (specTrans)
+        m[1:, 17] = 1.5                      # ior
+        m[1:, 18] = 0.6                      # atDistance
+        m[1:, 20:23] = [0.3, 0.55, 0.85]     # extinction
+        a["materials"] = m
     if name == "cornell_lights":
         p.enable_rr = 0
         p.max_depth = 5
@@ -128,7 +140,43 @@ CASES = {
     "icospheres": 2,
     "icospheres_constbg_tiled": 1,
     "icospheres_lens": 1,
+    "icospheres_absorb": 2,
 }
+
+
+def post_settings():
+    """Display-pass settings of the post-process golden vectors: every tone map with
+    RenderOptions' defaults, then vignette, chromatic aberration (offset and distortion forms),
+    both together, and the preview path."""
+    out = []
+    for t in range(7):
+        out.append(lf.PostParams.defaults(t))
+    p = lf.PostParams.defaults(2)
+    p.use_vignette, p.vignette_intensity, p.vignette_power = 1, 0.7, 1.5
+    out.append(p)
+    p = lf.PostParams.defaults(3)
+    p.use_ca, p.ca_distance = 1, 0.5
+    out.append(p)
+    p = lf.PostParams.defaults(1)
+    p.use_ca, p.use_ca_distortion, p.ca_distance = 1, 1, 0.8
+    out.append(p)
+    p = lf.PostParams.defaults(6)
+    p.use_ca, p.use_ca_distortion, p.ca_distance, p.ca_p1, p.ca_p2, p.ca_p3 = 1, 1, 0.6, 2.0, 1.5, 0.4
+    p.use_vignette, p.vignette_intensity, p.vignette_power = 1, 0.5, 2.5
+    out.append(p)
+    p = lf.PostParams.defaults(4)
+    p.use_ca, p.preview = 1, 1                     # preview ignores chromatic aberration
+    out.append(p)
+    return out
+
+
+POST_SAMPLES = 16
+
+
+def post_input():
+    """Accumulated sum over POST_SAMPLES samples fed to the display pass (24 x 40 RGB)."""
+    rng = np.random.default_rng(0)
+    return (rng.gamma(1.5, 1.0, (24, 40, 3)) * POST_SAMPLES).astype(np.float32)
 
 
 def stored_params(meta_case):

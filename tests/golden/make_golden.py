@@ -4,7 +4,9 @@ Every case (tests/golden/cases.py) is rebuilt with the reference's own host code
 and flatten, oracle/_ref/libref_host.so) and rendered with the reference's own GLSL shader
 compiled for the CPU (oracle/_ref/libref_shader.so, see oracle/ref_shader_gen.py). The stored
 per-path radiance pins the oracle and the CUDA path; the stored array digests pin the
-product's host scene layer. Needs a reference checkout:
+product's host scene layer. tests/golden/postprocess.npz holds the reference's display pass
+(postprocess.glsl, compiled the same way) of one accumulation buffer under every tone map, CA
+and vignette setting of cases.post_settings(). Needs a reference checkout:
 
     python oracle/build_ref.py && python tests/golden/make_golden.py
 """
@@ -67,6 +69,16 @@ def main():
                       "mean_radiance": float(paths.mean())}
         print(name, paths.shape, float(paths.mean()))
     np.savez_compressed(ROOT / "tests" / "golden" / "shader_paths.npz", **out)
+    # display pass: the reference's postprocess.glsl compiled for the CPU, per setting
+    sh.refsh_postprocess.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+    acc = cases.post_input()
+    post = {"input": acc}
+    for k, q in enumerate(cases.post_settings()):
+        rgbf = np.zeros(acc.shape, np.float32)
+        sh.refsh_postprocess(acc.ctypes.data, acc.shape[1], acc.shape[0], C.addressof(q), cases.POST_SAMPLES,
+                             rgbf.ctypes.data)
+        post[f"setting{k}"] = rgbf
+    np.savez_compressed(ROOT / "tests" / "golden" / "postprocess.npz", **post)
     (ROOT / "tests" / "golden" / "scenes.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
 
 

@@ -18,6 +18,7 @@ class RefHost:
         R.ref_scene_build.restype = P
         R.ref_scene_build.argtypes = [C.c_int, P, P, P, C.c_int, P, P, P, C.c_int, P]
         R.ref_scene_free.argtypes = [P]
+        R.ref_scene_move_instances.argtypes = [P, C.c_int, P, P]
         R.ref_scene_array.restype = P
         R.ref_scene_array.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
         R.ref_scene_top_level_index.argtypes = [P]
@@ -65,6 +66,27 @@ class RefHost:
         out = self._arrays(h)
         self.R.ref_scene_free(h)
         return out
+
+    def build_and_move(self, mesh_counts, vertices, normals, inst_mesh, transforms, inst_mat, materials, new_xf,
+                       new_mat):
+        """Arrays of the scene built with the reference's code, then after Scene::RebuildInstances
+        with the instances' new transforms and materials."""
+        mc = np.ascontiguousarray(mesh_counts, np.int32)
+        v = np.ascontiguousarray(vertices, np.float32)
+        n = np.ascontiguousarray(normals, np.float32)
+        im = np.ascontiguousarray(inst_mesh, np.int32)
+        xf = np.ascontiguousarray(transforms, np.float32)
+        imat = np.ascontiguousarray(inst_mat, np.int32)
+        mats = np.ascontiguousarray(materials, np.float32)
+        h = self.R.ref_scene_build(len(mc), mc.ctypes.data, v.ctypes.data, n.ctypes.data, len(im), im.ctypes.data,
+                                   xf.ctypes.data, imat.ctypes.data, len(mats), mats.ctypes.data)
+        before = self._arrays(h)
+        nx = np.ascontiguousarray(new_xf, np.float32)
+        nm = np.ascontiguousarray(new_mat, np.int32)
+        self.R.ref_scene_move_instances(h, len(nm), nx.ctypes.data, nm.ctypes.data)
+        after = self._arrays(h)
+        self.R.ref_scene_free(h)
+        return before, after
 
     def camera(self, eye, at, fov):
         out = np.zeros(15, np.float32)

@@ -36,3 +36,18 @@ def test_oracle_paths_equal_reference_shader(name):
     assert paths.shape == gold.shape
     same = np.all((paths == gold) | (np.isnan(paths) & np.isnan(gold)), axis=-1)
     assert same.all(), f"{(~same).sum()} of {same.size} paths differ"
+
+
+def test_oracle_postprocess_equals_reference_shader():
+    """The display pass (postprocess.glsl:126-171 with TiledRenderer's uniforms) against the
+    reference shader compiled for the CPU: every tone map, CA form, vignette and the preview
+    path, bit for bit."""
+    gold = np.load(GOLD / "postprocess.npz")
+    acc = gold["input"]
+    settings = cases.post_settings()
+    assert len(gold.files) == len(settings) + 1
+    for k, q in enumerate(settings):
+        _, rgbf = oracle.postprocess(acc, q, cases.POST_SAMPLES)
+        ref = gold[f"setting{k}"]
+        same = (rgbf.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(rgbf) & np.isnan(ref))
+        assert same.all(), f"setting {k} (tone map {q.tonemap}): {(~same).sum()} values differ"

@@ -235,7 +235,7 @@ def test_invalid_scene_view_is_rejected(ctx):
 
 
 @pytest.mark.parametrize("name", ["cornell", "cornell_lights", "cornell_textures", "room", "icospheres",
-                                  "icospheres_constbg_tiled", "icospheres_lens"])
+                                  "icospheres_constbg_tiled", "icospheres_lens", "icospheres_absorb"])
 def test_gpu_paths_equal_reference_shader(ctx, name):
     """Device paths against the reference GLSL shader compiled for the CPU (golden vectors)."""
     import json
@@ -316,4 +316,61 @@ def test_equal_distance_hits_follow_the_reference_order(ctx):
     for flags in (0, lf.TRACE_SIMPLE):
         dev = ctx.trace_closest(ds, rays, flags=flags)
         assert compare_hits(dev, ref) == 0
+    ds.close()
+
+
+def move_all(s, seed):
+    """Moves every instance of a built host scene (new transforms, materials kept) and runs
+    Scene::RebuildInstances."""
+    from tests.test_scene_reference import moved_instances
+
+    new_xf = moved_instances(s.arrays(), seed)
+    _, _, inst_mat = s.layout()
+    for i in range(len(new_xf)):
+        s.set_instance(i, new_xf[i], int(inst_mat[i]))
+    s.rebuild_instances()
+
+
+def test_instance_update_ray_queries_match_oracle(ctx):
+    """lf_scene_update_instances (Renderer::Update's partial re-upload, Renderer.cpp:190-205)
+    after Scene::RebuildInstances: queries on the updated device scene equal the oracle on the
+    moved scene, and equal a fresh upload of it."""
+    s = lf.HostScene().gen_soup(1 << 12, 10, 3).build()
+    ds = ctx.upload(s)
+    rays = soup_rays(s, 1 << 16, seed=5)
+    before = ctx.trace_closest(ds, rays)
+    move_all(s, 9)
+    ds.update_instances(s)
+    dev = ctx.trace_closest(ds, rays)
+    ref, _ = oracle.trace_closest(s.view(), rays)
+    assert compare_hits(dev, ref) == 0
+    assert compare_hits(before, ref) > 1000          # the move changed the answers
+    occ = ctx.trace_any(ds, rays)
+    ref_occ, _ = oracle.trace_any(s.view(), rays)
+    assert np.array_equal(occ, ref_occ)
+    fresh = ctx.upload(s)
+    assert ctx.trace_closest(fresh, rays).tobytes() == dev.tobytes()
+    fresh.close()
+    ds.close()
+
+
+def test_instance_update_render_matches_oracle(ctx):
+    s = lf.HostScene().gen_icospheres(6, 3, 5, 64, 32).build()
+    p = s.render_params()
+    p.width, p.height = 64, 36
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p)
+    f.render(0, 2)
+    f.sync()
+    before = f.paths(2)
+    move_all(s, 4)
+    ds.update_instances(s)
+    f.reset()                       # the frame that rendered before the move continues
+    f.render(0, 2)
+    f.sync()
+    ref_acc, ref_paths, _ = oracle.render(s.view(), p, 0, 2, want_paths=True)
+    assert_paths_match(f.paths(2), ref_paths) == 1.0
+    assert f.accum().tobytes() == ref_acc.tobytes()
+    assert before.tobytes() != ref_paths.tobytes()
+    f.close()
     ds.close()

@@ -66,19 +66,9 @@ def np_post(acc, p, samples):
 
 
 def settings():
-    out = []
-    for t in range(7):
-        out.append(lf.PostParams.defaults(t))
-    p = lf.PostParams.defaults(2)
-    p.use_vignette, p.vignette_intensity, p.vignette_power = 1, 0.7, 1.5
-    out.append(p)
-    p = lf.PostParams.defaults(3)
-    p.use_ca, p.ca_distance = 1, 0.5
-    out.append(p)
-    p = lf.PostParams.defaults(1)
-    p.use_ca, p.use_ca_distortion, p.ca_distance = 1, 1, 0.8
-    out.append(p)
-    return out
+    from tests.golden.cases import post_settings
+
+    return post_settings()
 
 
 def test_oracle_postprocess_matches_the_shader_formulas():

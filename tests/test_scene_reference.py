@@ -101,3 +101,40 @@ def test_camera_matches_reference(eye, at, fov, ref_host):
     cam = np.concatenate([p.cam_position, p.cam_right, p.cam_up, p.cam_forward,
                           [p.cam_fov, p.cam_focal_dist, p.cam_aperture]]).astype(np.float32)
     assert cam.tobytes() == r.tobytes()
+
+
+def moved_instances(a, seed):
+    """New transforms (each instance shifted, every third also turned about its own z axis)
+    and permuted materials for every instance of a built scene."""
+    rng = np.random.default_rng(seed)
+    xf = a["transforms"].reshape(-1, 4, 4).astype(np.float32).copy()
+    ext = float(np.abs(a["nodes"][:, :6]).max())
+    for i in range(len(xf)):
+        xf[i, 3, :3] += rng.uniform(-0.1, 0.1, 3).astype(np.float32) * np.float32(ext)
+        if i % 3 == 0:
+            c, s_ = np.cos(0.4 + i), np.sin(0.4 + i)
+            rot = np.array([[c, s_, 0], [-s_, c, 0], [0, 0, 1]], np.float32)
+            xf[i, :3, :3] = (rot @ xf[i, :3, :3]).astype(np.float32)
+    return xf.reshape(-1, 16)
+
+
+@pytest.mark.parametrize("gen", ["soup", "icospheres"])
+def test_instance_move_matches_reference_rebuild(gen, ref_host):
+    """Scene::RebuildInstances after instances move (Scene.cpp:165-178, BvhTranslator::UpdateTLAS
+    bvh_translator.cpp:125-131): the rebuilt TLAS part of the node array and the transforms must
+    be byte-identical to the reference's."""
+    s = scenes.build(gen)
+    a = s.arrays()
+    counts, inst_mesh, inst_mat = s.layout()
+    new_xf = moved_instances(a, 7)
+    n_mat = a["materials"].shape[0]
+    new_mat = (np.asarray(inst_mat) + 1) % n_mat
+    before, after = ref_host.build_and_move(counts, a["vertices"], a["normals"], inst_mesh, a["transforms"], inst_mat,
+                                            a["materials"], new_xf, new_mat)
+    assert_same(a, before, keys=["nodes", "transforms"])
+    for i in range(len(new_mat)):
+        s.set_instance(i, new_xf[i], int(new_mat[i]))
+    s.rebuild_instances()
+    b = s.arrays()
+    assert b["nodes"].tobytes() != a["nodes"].tobytes()
+    assert_same(b, after, keys=["nodes", "vert_indices", "vertices", "normals", "transforms", "materials"])
