@@ -151,6 +151,9 @@ lf_status lf_hscene_render_params(const lf_hscene* s, lf_render_params* out);
 
 /* Procedural workloads (seeded, deterministic on every host). */
 lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height);
+/* The same box with every wall and box face split into subdiv x subdiv quads (34 subdiv^2
+ * triangles): the Cornell generator scaled for the serving mix. */
+lf_status lf_gen_cornell_tess(lf_hscene* s, int32_t width, int32_t height, int32_t subdiv);
 lf_status lf_gen_soup(lf_hscene* s, int32_t instances, int32_t tris_per_instance, uint64_t seed);
 lf_status lf_gen_icospheres(lf_hscene* s, int32_t instances, int32_t level, uint64_t seed, int32_t env_width,
                             int32_t env_height);
@@ -223,6 +226,14 @@ lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64
  * leaf visits (sums over all rays). */
 lf_status lf_trace_stats(const lf_ctx* c, uint64_t out3[3]);
 
+/* Traversal-kernel timer (no counterpart in the reference; measurement aid): while on, the
+ * device ray queries (lf_trace_closest_device / lf_trace_any_device, binned path) record a
+ * CUDA event pair on the context's stream around the traversal kernel alone. _read waits for
+ * the recorded launches and returns their summed duration and count, then starts over. */
+lf_status lf_ctx_kernel_timer(lf_ctx* c, int32_t on);
+/* Streaming multiprocessors and maximum SM clock (MHz) of the context's device. */
+lf_status lf_ctx_device_attrs(lf_ctx* c, int32_t* sm_count, int32_t* max_sm_mhz);
+lf_status lf_ctx_kernel_timer_read(lf_ctx* c, double* total_ms, int64_t* launches);
 /* Page-locked host memory, mapped into the device's address space (fast host<->device
  * copies; host queries write their results straight into it), e.g. for ray and hit buffers. */
 lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out);
@@ -281,6 +292,14 @@ lf_status lf_frame_release(lf_frame* f);
  * while passes are in flight. */
 lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend, int32_t block_shade,
                                   int32_t block_shadow, int32_t shade_threads_per_sm);
+/* Sort-by-material in the engine (no counterpart in the reference, whose shader shades each
+ * fragment where it lands, pathtrace.glsl:246-291): 1 = the extend kernel buckets the paths
+ * that hit a surface by the class of their material's shading code (opaque dielectric, metal,
+ * transmissive, textured) and shade takes the buckets one after the other, so that a warp
+ * runs one class; 0 (default) = hits in the order extend finished them. Results are
+ * unchanged either way. The buckets take 16 B per path slot, allocated on first use. Fails
+ * with LF_ERR_STATE while passes are in flight. */
+lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material);
 /* Current pool size and device bytes of the engine (0, 0 before first use). */
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 

@@ -53,6 +53,7 @@ _SIG = {
     "lf_hscene_layout": (C.c_int, [_P, _I, _I, _I]),
     "lf_hscene_render_params": (C.c_int, [_P, _P]),
     "lf_gen_cornell": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "lf_gen_cornell_tess": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "lf_gen_soup": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64]),
     "lf_gen_icospheres": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.c_int32]),
     "lf_gen_room": (C.c_int, [_P, C.c_int32, C.c_uint64]),
@@ -66,6 +67,10 @@ _SIG = {
     "lf_ctx_timer_stop": (C.c_int, [_P, _F]),
     "lf_ctx_configure_engine": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "lf_ctx_set_host_chunks": (C.c_int, [_P, C.c_int32]),
+    "lf_ctx_set_engine_sort": (C.c_int, [_P, C.c_int32]),
+    "lf_ctx_kernel_timer": (C.c_int, [_P, C.c_int32]),
+    "lf_ctx_device_attrs": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "lf_ctx_kernel_timer_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "lf_ctx_engine_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "lf_scene_upload": (C.c_int, [_P, _P, C.POINTER(_P)]),
     "lf_scene_update_instances": (C.c_int, [_P, _P]),
@@ -305,8 +310,12 @@ class HostScene:
         return mc, im, imat
 
     # procedural workloads
-    def gen_cornell(self, width=256, height=256):
-        self._c(lib().lf_gen_cornell(self.h, width, height))
+    def gen_cornell(self, width=256, height=256, subdiv=1):
+        """Procedural Cornell box; subdiv > 1 splits every face into subdiv^2 quads."""
+        if subdiv == 1:
+            self._c(lib().lf_gen_cornell(self.h, width, height))
+        else:
+            self._c(lib().lf_gen_cornell_tess(self.h, width, height, subdiv))
         return self
 
     def gen_soup(self, instances, tris_per_instance, seed=1):
@@ -373,6 +382,27 @@ class Context:
         (0 = keep the pool / default)."""
         self._c(lib().lf_ctx_configure_engine(self.h, slots, block_extend, block_shade, block_shadow,
                                               shade_threads_per_sm))
+
+    def device_attrs(self):
+        """{"sm_count", "max_sm_mhz"} of the context's device."""
+        n, mhz = C.c_int32(), C.c_int32()
+        self._c(lib().lf_ctx_device_attrs(self.h, C.byref(n), C.byref(mhz)))
+        return {"sm_count": n.value, "max_sm_mhz": mhz.value}
+
+    def kernel_timer(self, on):
+        """Times the traversal kernel of the device ray queries alone (CUDA events)."""
+        self._c(lib().lf_ctx_kernel_timer(self.h, 1 if on else 0))
+
+    def kernel_timer_read(self):
+        """(summed milliseconds, launches) of the traversal kernels timed since the last read."""
+        ms, n = C.c_double(), C.c_int64()
+        self._c(lib().lf_ctx_kernel_timer_read(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def set_engine_sort(self, sort_by_material):
+        """Engine sort-by-material: shade takes the paths that hit a surface grouped by the class
+        of their material (results unchanged)."""
+        self._c(lib().lf_ctx_set_engine_sort(self.h, 1 if sort_by_material else 0))
 
     def set_host_chunks(self, chunks=0):
         """Pieces of host-buffer ray queries whose copies overlap tracing (0 = automatic)."""

@@ -600,6 +600,55 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
     return nh;
 }
 
+constexpr int kWideBlasEnd = (int)0x80000000;   // stack marker: leave the instance
+constexpr int kWideNone = (int)0x80000001;      // no next node
+
+// Occlusion form of wide_node: any-hit returns a boolean, so the order in which the children
+// are visited cannot change its answer (AnyHit, anyhit.glsl:7-173, accepts the first triangle
+// with t < maxDist it meets). The hit children are taken in slot order without keys or a
+// sorting network: the first is returned (kWideNone if none), the others are pushed. Returns
+// kWideEmpty, pushing nothing, when the pushes would overflow the stack.
+__device__ __forceinline__ int wide_node_any(const DevScene& S, int code, v3 ro, v3 invd, float lim, int* stack,
+                                             int& sp)
+{
+    const float4* rec = S.wnodes + (size_t)code * kWideF4;
+    constexpr int G = kWide / 4;
+    float g[7][kWide];
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+#pragma unroll
+        for (int h4 = 0; h4 < G; ++h4)
+        {
+            const float4 f = ldg4(rec + q * G + h4);
+            g[q][h4 * 4 + 0] = f.x;
+            g[q][h4 * 4 + 1] = f.y;
+            g[q][h4 * 4 + 2] = f.z;
+            g[q][h4 * 4 + 3] = f.w;
+        }
+    bool hit[kWide];
+    int nh = 0;
+#pragma unroll
+    for (int j = 0; j < kWide; ++j)
+    {
+        const float fx = (g[1][j] - ro.x) * invd.x, fy = (g[3][j] - ro.y) * invd.y, fz = (g[5][j] - ro.z) * invd.z;
+        const float nx = (g[0][j] - ro.x) * invd.x, ny = (g[2][j] - ro.y) * invd.y, nz = (g[4][j] - ro.z) * invd.z;
+        const float t1 = fmin3_hw(fmaxf(fx, nx), fmaxf(fy, ny), fmaxf(fz, nz));
+        const float t0 = fmax3_hw(fminf(fx, nx), fminf(fy, ny), fminf(fz, nz));
+        hit[j] = t1 >= t0 && t1 > 0.f && fmaxf(t0, 0.f) <= lim;
+        nh += hit[j] ? 1 : 0;
+    }
+    if (sp + nh - 1 > kWideStack) return kWideEmpty;
+    int next = kWideNone;
+#pragma unroll
+    for (int j = 0; j < kWide; ++j)
+        if (hit[j])
+        {
+            if (next != kWideNone) stack[sp++] = next;
+            next = __float_as_int(g[6][j]);
+        }
+    return next;
+}
+
 // Two-level traversal of the wide tree as a state machine: wide_step visits one node or leaf
 // and folds the stack pop into the same step. Leaves are triangle runs on the mesh level and
 // instances on the instance level; entering an instance pushes a marker and switches to the
@@ -617,8 +666,6 @@ struct WideRay
     uint32_t err;
 };
 
-constexpr int kWideBlasEnd = (int)0x80000000;   // stack marker: leave the instance
-constexpr int kWideNone = (int)0x80000001;
 
 // Starts a traversal of a ray with a regular inverse direction (inv_dir's `fast`).
 __device__ __forceinline__ void wide_init(const DevScene& S, WideRay& w, v3 o, v3 d, v3 winvd, float tmax)
@@ -648,7 +695,17 @@ __device__ __forceinline__ bool wide_step(const DevScene& S, WideRay& w, int* st
         return true;
     }
     int code = w.code;
-    if (code >= 0)
+    if (kAny && code >= 0)
+    {
+        const float lim = S.cullRel >= 0.f ? w.t + w.t * S.cullRel + S.cullAbs : 3.4e38f;
+        code = wide_node_any(S, code, w.ro, w.invd, lim, stack, w.sp);
+        if (code == kWideEmpty)
+        {
+            w.err |= LF_DEVERR_STACK;
+            return true;
+        }
+    }
+    else if (code >= 0)
     {
         int hc[kWide];
         const float lim = S.cullRel >= 0.f ? w.t + w.t * S.cullRel + S.cullAbs : 3.4e38f;

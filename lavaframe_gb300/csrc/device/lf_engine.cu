@@ -123,6 +123,7 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
     c->refillNext = 0;
     c->hitCount = 0;
     c->missCount = 0;
+    for (int k = 0; k < 4; ++k) c->bucketCount[k] = 0;
 }
 
 // ------------------------------------------------------------------ finish / refill
@@ -253,24 +254,55 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
         const int i = base + lane;
         int p = -1;
         bool miss = false;
+        int cls = 0;
         if (i < n)
         {
             p = q[i];
             const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
             Hit h;
             uint32_t err;
+            const ShadeInstance* sinst;
             if constexpr (kOne)
+            {
                 err = closest_hit<false>(one.S.trav, f3(o4), f3(d4), kInfinity, one.P.useLights != 0, &h, nullptr);
+                sinst = one.S.inst;
+            }
             else
             {
                 const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
                 const EngineJob& J = b.jobs[job_of(w)];
                 const DevScene T = J.S.trav;
                 err = closest_hit<false>(T, f3(o4), f3(d4), kInfinity, J.P.useLights != 0, &h, nullptr);
+                sinst = J.S.inst;
             }
             b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
             set_error(b.status, err);
             miss = h.t == kInfinity;   // the shade kernel's environment case
+            if (b.sortByMaterial && !miss && h.inst >= 0) cls = sinst[h.inst].shadeClass & 3;
+        }
+        if (b.sortByMaterial)
+        {
+            // hits go to the bucket of their material class, misses to the back of `part`
+            const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                const unsigned km = __ballot_sync(kFull, p >= 0 && !miss && cls == k);
+                int kb = 0;
+                if (lane == 0 && km) kb = atomicAdd(&b.ctl->bucketCount[k], __popc(km));
+                kb = __shfl_sync(kFull, kb, 0);
+                if (p >= 0 && !miss && cls == k) b.partSort[(size_t)k * b.cap + kb + __popc(km & below)] = p;
+            }
+            const unsigned hm = __ballot_sync(kFull, p >= 0 && !miss), mm = __ballot_sync(kFull, p >= 0 && miss);
+            int mb = 0;
+            if (lane == 0)
+            {
+                if (hm) atomicAdd(&b.ctl->hitCount, __popc(hm));
+                if (mm) mb = atomicAdd(&b.ctl->missCount, __popc(mm));
+            }
+            mb = __shfl_sync(kFull, mb, 0);
+            if (p >= 0 && miss) b.part[b.cap - 1 - (mb + __popc(mm & below))] = p;
+            continue;
         }
         // hits count up from the front of `part`, misses down from the back; together they
         // are the n queued paths, so the two ranges never meet
@@ -316,7 +348,17 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
         ShadowRec rec;
         if (i < n)
         {
-            p = i < nHit ? b.part[i] : b.part[b.cap - 1 - (i - nHit)];
+            if (i >= nHit)
+                p = b.part[b.cap - 1 - (i - nHit)];
+            else if (!b.sortByMaterial)
+                p = b.part[i];
+            else
+            {
+                // hits class by class: find the bucket of position i
+                int k = 0, off = i;
+                while (k < 3 && off >= ctl->bucketCount[k]) off -= ctl->bucketCount[k++];
+                p = b.partSort[(size_t)k * b.cap + off];
+            }
             if constexpr (kOne)
                 shade_path<kLights>(one.S, one.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
             else
@@ -348,12 +390,12 @@ __global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob 
         if (base >= n) break;
         const int i = base + lane;
         if (i >= n) continue;
-        const ShadowRec rec = b.shadow[i];
+        const ShadowRec* rec = b.shadow + i;
         if constexpr (kOne)
             set_error(b.status, shadow_path(one.S, one.P, b.ps, rec, rays));
         else
         {
-            const int p = __float_as_int(rec.a.w);
+            const int p = __float_as_int(rec->a.w);
             const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
             const EngineJob& J = b.jobs[job_of(w)];
             set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, rays));
@@ -384,7 +426,7 @@ __device__ __forceinline__ void drain_path(const EngineBuffers& b, const EngineJ
         bool pushExt = false, pushShadow = false;
         ShadowRec rec;
         shade_path(J.S, J.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
-        if (pushShadow) set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, shadowRays));
+        if (pushShadow) set_error(b.status, shadow_path(J.S, J.P, b.ps, &rec, shadowRays));
         if (!pushExt) return;
     }
 }

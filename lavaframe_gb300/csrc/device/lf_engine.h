@@ -13,7 +13,8 @@
 //   finish   done[k]: write out finished paths, count pass completions, free their slots
 //   refill   start new paths in free slots while unissued ids remain (-> queue[k])
 //   reset    commit the refill, clear done[k], the shadow queue and queue[k^1]
-//   extend   closest hit of every queued path; hits and misses -> part (front and back)
+//   extend   closest hit of every queued path; hits and misses -> part (front and back), or
+//            with sort-by-material the hits into one bucket per material class
 //   shade    one PathTrace bounce over part's hits, then its misses, so that a warp shades
 //            one kind; survivors -> queue[k^1], finished -> done[k^1]
 //   shadow   next-event visibility
@@ -59,6 +60,7 @@ struct EngineCtl
     int extendNext, shadeNext, shadowNext;   // work counters of the extend, shade and shadow kernels
     int refillNext;                // ids handed out by the current refill
     int hitCount, missCount;       // the extension queue split by extend: hits, then misses
+    int bucketCount[4];            // sort-by-material: hits per material class
 };
 
 struct EngineBuffers
@@ -66,6 +68,8 @@ struct EngineBuffers
     PathSoA ps;                  // info: x radiance entry in the pass, y depth, z last material, w ring | job << 14
     int* queue[2];
     int* part;                   // extended paths: hits from the front, misses from the back
+    int* partSort;               // sort-by-material: hits of class k at [k * cap, k * cap + bucketCount[k])
+    int sortByMaterial;          // 1: extend buckets hits by material class, shade takes them class by class
     ShadowRec* shadow;
     int* done[2];                // slots whose path finished
     EngineCtl* ctl;

@@ -28,6 +28,7 @@ void free_engine_buffers(EngineHost* e)
     drop_graphs(e);
     for (void* p : e->allocs) cudaFree(p);
     e->allocs.clear();
+    e->b.partSort = nullptr;
 }
 
 lf_status alloc_pool(EngineHost* e, int slots)
@@ -54,6 +55,7 @@ lf_status alloc_pool(EngineHost* e, int slots)
     A(&b.done[0], slots);
     A(&b.done[1], slots);
     A(&b.shadow, slots);
+    if (b.sortByMaterial) A(&b.partSort, (size_t)4 * slots);
     if (err != cudaSuccess)
     {
         free_engine_buffers(e);
@@ -167,6 +169,23 @@ lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockS
         if (st != LF_OK) return st;
         if (launch_engine_init(e->b, c->stream) != 0) return fail(c, LF_ERR_CUDA, "engine init launch");
     }
+    return LF_OK;
+}
+
+lf_status engine_set_sort(EngineHost* e, bool on)
+{
+    lf_ctx* c = e->c;
+    if (e->active > 0) return fail(c, LF_ERR_STATE, "engine has passes in flight");
+    cudaStreamSynchronize(c->stream);
+    if (on && !e->b.partSort)
+    {
+        size_t bytes = 0;
+        cudaError_t err = dalloc(e->allocs, bytes, &e->b.partSort, (size_t)4 * e->b.cap);
+        if (err != cudaSuccess) return cuda_fail(c, err, "sort-by-material buckets");
+        e->poolBytes += bytes;
+    }
+    e->b.sortByMaterial = on ? 1 : 0;
+    drop_graphs(e);   // the graphs hold the kernel parameters
     return LF_OK;
 }
 

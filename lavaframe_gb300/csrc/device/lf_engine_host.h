@@ -42,6 +42,9 @@ lf_status engine_get(lf_ctx* c, EngineHost** out);
 // and the register cap of shade (threads per SM it must fit: 0 none, 512, 768, 1024).
 lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockShade, int blockShadow,
                            int shadeThreadsPerSm);
+// Sort-by-material on or off: extend buckets the hits by material class (4 x slots queue
+// entries, allocated on first use) and shade takes them class by class.
+lf_status engine_set_sort(EngineHost* e, bool on);
 int engine_job_alloc(EngineHost* e, const ShadeScene& S, const Params& P);
 void engine_job_write(EngineHost* e, int job, const ShadeScene& S, const Params& P);
 void engine_job_free(EngineHost* e, int job);

@@ -60,6 +60,10 @@ struct lf_ctx
     uint32_t* binHist = nullptr;
     unsigned long long* binNext = nullptr;
     lfrt::EngineHost* engine = nullptr;   // multi-job engine, created on first use
+    // traversal-kernel timer of the binned ray queries: one event pair per launch while on
+    bool kernelTimer = false;
+    std::vector<cudaEvent_t> ktEvents;     // start, stop, start, stop, ...
+    size_t ktUsed = 0;                     // pairs recorded since the last read
 };
 
 struct lf_scene

@@ -126,7 +126,7 @@ __global__ void __maxnreg__(72) shadow_kernel(ShadeScene S, Params P, PathSoA ps
         base = __shfl_sync(kFull, base, 0);
         if (base >= (unsigned long long)n) break;
         const int i = (int)base + lane;
-        if (i < n) set_error(status, shadow_path(S, P, ps, sq[i], rays));
+        if (i < n) set_error(status, shadow_path(S, P, ps, sq + i, rays));
     }
     warp_count_add(&ctr[2], rays);
 }

@@ -79,9 +79,11 @@ int launch_accumulate(const Params& P, const PathSoA& ps, int nSamples, float4* 
                       cudaStream_t st);
 int launch_trace_closest(const DevScene& S, const float4* rays, long long n, int4* hits, int lights, bool stats,
                          uint32_t* status, unsigned long long* stat3, cudaStream_t st);
+// evStart / evStop (optional) are recorded on `st` around the traversal kernel alone.
 int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void* out, bool any, int lights,
                         const float lo[3], const float hi[3], bool binning, uint32_t* keys, uint32_t* hist, int* perm,
-                        unsigned long long* next, uint32_t* status, cudaStream_t st);
+                        unsigned long long* next, uint32_t* status, cudaStream_t st, cudaEvent_t evStart = nullptr,
+                        cudaEvent_t evStop = nullptr);
 int trace_bins();
 int launch_trace_any(const DevScene& S, const float4* rays, long long n, uint8_t* occ, int lights, bool stats,
                      uint32_t* status, unsigned long long* stat3, cudaStream_t st);

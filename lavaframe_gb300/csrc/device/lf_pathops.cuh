@@ -437,15 +437,18 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
 }
 
 // Visibility of a path's next-event rays, then radiance += Li * throughput
-// (pathtrace.glsl:126-204, 266). Returns device error bits; counts traced rays.
+// (pathtrace.glsl:126-204, 266). Returns device error bits; counts traced rays. The record is
+// read field by field where it is used (a queued record in global memory, or the drain's own),
+// so that only the position, the path, the flags and Li stay live across the traversals.
 __device__ __forceinline__ uint32_t shadow_path(const ShadeScene& S, const Params& P, const PathSoA& ps,
-                                                const ShadowRec& rec, unsigned long long& rays)
+                                                const ShadowRec* rec, unsigned long long& rays)
 {
     using namespace pathops;
     const bool lights = P.useLights != 0;
-    int p = __float_as_int(rec.a.w);
-    uint32_t flags = __float_as_uint(rec.b.w);
-    v3 pos = f3(rec.a);
+    const float4 a4 = rec->a;
+    const int p = __float_as_int(a4.w);
+    const uint32_t flags = __float_as_uint(rec->b.w);
+    const v3 pos = f3(a4);
     v3 Li(0.0f);
     Hit h;
     bool occ;
@@ -456,14 +459,18 @@ __device__ __forceinline__ uint32_t shadow_path(const ShadeScene& S, const Param
     for (int j = 0; j < nr; ++j)
     {
         const bool env = (flags & 1u) && j == 0;
-        const float4 dir = env ? rec.c : rec.f;
-        const float4 col = env ? rec.e : rec.g;
-        err |= any_hit<false>(S.trav, pos, f3(dir), env ? kInfinity - kEps : rec.f.w, lights, &occ, &h, nullptr);
-        if (!occ) Li = Li + f3(col);
+        const float4 dir = env ? rec->c : rec->f;
+        err |= any_hit<false>(S.trav, pos, f3(dir), env ? kInfinity - kEps : dir.w, lights, &occ, &h, nullptr);
+        if (!occ)
+        {
+            const float4 col = env ? rec->e : rec->g;
+            Li = Li + f3(col);
+        }
         ++rays;
     }
+    const float4 T4 = rec->b;
     float4 L4 = ps.L[p];
-    v3 L = f3(L4) + Li * f3(rec.b);
+    v3 L = f3(L4) + Li * f3(T4);
     ps.L[p] = f4(L, 0.f);
     return err;
 }

@@ -63,6 +63,7 @@ void lf_ctx_destroy(lf_ctx* c)
         if (c->chunkIn[k]) cudaEventDestroy(c->chunkIn[k]);
         if (c->chunkDone[k]) cudaEventDestroy(c->chunkDone[k]);
     }
+    for (cudaEvent_t ev : c->ktEvents) cudaEventDestroy(ev);
     if (c->chunkStart) cudaEventDestroy(c->chunkStart);
     if (c->chunkEnd) cudaEventDestroy(c->chunkEnd);
     if (c->copyIn) cudaStreamDestroy(c->copyIn);
@@ -102,6 +103,47 @@ lf_status lf_ctx_timer_stop(lf_ctx* c, float* ms)
     if (e == cudaSuccess) e = cudaEventSynchronize(c->ev[1]);
     if (e == cudaSuccess) e = cudaEventElapsedTime(ms, c->ev[0], c->ev[1]);
     return e == cudaSuccess ? LF_OK : cuda_fail(c, e, "event timing");
+}
+
+lf_status lf_ctx_device_attrs(lf_ctx* c, int32_t* sm_count, int32_t* max_sm_mhz)
+{
+    if (!c || !sm_count || !max_sm_mhz) return LF_ERR_INVALID;
+    int sms = 0, khz = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "device attributes");
+    *sm_count = sms;
+    *max_sm_mhz = khz / 1000;
+    return LF_OK;
+}
+
+lf_status lf_ctx_kernel_timer(lf_ctx* c, int32_t on)
+{
+    if (!c) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    c->kernelTimer = on != 0;
+    c->ktUsed = 0;
+    return LF_OK;
+}
+
+lf_status lf_ctx_kernel_timer_read(lf_ctx* c, double* total_ms, int64_t* launches)
+{
+    if (!c || !total_ms || !launches) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    double sum = 0.0;
+    for (size_t k = 0; k < c->ktUsed; ++k)
+    {
+        cudaError_t e = cudaEventSynchronize(c->ktEvents[2 * k + 1]);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ktEvents[2 * k], c->ktEvents[2 * k + 1]);
+        if (e != cudaSuccess) return cuda_fail(c, e, "kernel timer");
+        sum += ms;
+    }
+    *total_ms = sum;
+    *launches = (int64_t)c->ktUsed;
+    c->ktUsed = 0;
+    return LF_OK;
 }
 
 lf_status lf_host_alloc(lf_ctx* c, size_t bytes, void** out)
@@ -554,6 +596,11 @@ lf_status encode_instances(lf_ctx* c, const lf_scene_view* v, const RefNode* nod
             for (int r = 0; r < 3; ++r) s.fwd[col * 3 + r] = M[col * 4 + r];
         lfc::normal_matrix(M, s.nrm);
         s.material = mat;
+        // class of the material's shading code (Material.h layout: metallic [8], transmission
+        // [16], texture ids [24..27]) for the engine's sort-by-material
+        const float* mp = v->materials + (size_t)mat * 28;
+        const bool textured = mp[24] >= 0.f || mp[25] >= 0.f || mp[26] >= 0.f || mp[27] >= 0.f;
+        s.shadeClass = textured ? 3 : mp[16] > 0.f ? 2 : mp[8] >= 0.5f ? 1 : 0;
     }
     return LF_OK;
 }
@@ -866,6 +913,22 @@ lf_status ensure_bin_scratch(lf_ctx* c, long long n)
 }
 }
 
+// Next event pair of the traversal-kernel timer (nullptr, nullptr when it is off).
+void kernel_timer_pair(lf_ctx* c, cudaEvent_t* a, cudaEvent_t* b)
+{
+    *a = *b = nullptr;
+    if (!c->kernelTimer) return;
+    while (c->ktEvents.size() < 2 * (c->ktUsed + 1))
+    {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreate(&ev) != cudaSuccess) return;
+        c->ktEvents.push_back(ev);
+    }
+    *a = c->ktEvents[2 * c->ktUsed];
+    *b = c->ktEvents[2 * c->ktUsed + 1];
+    ++c->ktUsed;
+}
+
 extern "C" {
 
 lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64_t n, void* d_hits, uint32_t flags)
@@ -881,9 +944,11 @@ lf_status lf_trace_closest_device(lf_ctx* c, lf_scene* sc, const void* d_rays, i
     {
         lf_status bs = ensure_bin_scratch(c, n);
         if (bs != LF_OK) return bs;
+        cudaEvent_t k0, k1;
+        kernel_timer_pair(c, &k0, &k1);
         e = launch_trace_binned(sc->view.trav, (const float4*)d_rays, n, d_hits, false, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
                                 sc->boundsLo, sc->boundsHi, !(flags & LF_TRACE_UNSORTED), c->binKeys, c->binHist,
-                                c->binPerm, c->binNext, c->d_status, c->stream);
+                                c->binPerm, c->binNext, c->d_status, c->stream, k0, k1);
     }
     else
         e = launch_trace_closest(sc->view.trav, (const float4*)d_rays, n, (int4*)d_hits, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
@@ -905,9 +970,11 @@ lf_status lf_trace_any_device(lf_ctx* c, lf_scene* sc, const void* d_rays, int64
     {
         lf_status bs = ensure_bin_scratch(c, n);
         if (bs != LF_OK) return bs;
+        cudaEvent_t k0, k1;
+        kernel_timer_pair(c, &k0, &k1);
         e = launch_trace_binned(sc->view.trav, (const float4*)d_rays, n, d_occ, true, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
                                 sc->boundsLo, sc->boundsHi, !(flags & LF_TRACE_UNSORTED), c->binKeys, c->binHist,
-                                c->binPerm, c->binNext, c->d_status, c->stream);
+                                c->binPerm, c->binNext, c->d_status, c->stream, k0, k1);
     }
     else
         e = launch_trace_any(sc->view.trav, (const float4*)d_rays, n, (uint8_t*)d_occ, (flags & LF_TRACE_LIGHTS) ? 1 : 0,
@@ -1634,6 +1701,17 @@ lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend
     lf_status st = engine_get(c, &e);
     if (st != LF_OK) return st;
     return engine_configure(e, slots, block_extend, block_shade, block_shadow, shade_threads_per_sm);
+}
+
+lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material)
+{
+    if (!c || sort_by_material < 0 || sort_by_material > 1) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    EngineHost* e = nullptr;
+    lf_status st = engine_get(c, &e);
+    if (st != LF_OK) return st;
+    return engine_set_sort(e, sort_by_material != 0);
 }
 
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes)

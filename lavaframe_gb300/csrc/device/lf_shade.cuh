@@ -49,7 +49,8 @@ struct ShadeInstance
     float fwd[12];   // forward transform columns 0..3 (xyz)
     float nrm[9];    // transpose(inverse(mat3(M))), column-major
     int material;
-    float pad[2];
+    int shadeClass;  // material class for sort-by-material: 0 opaque dielectric, 1 metal, 2 transmissive, 3 textured
+    float pad;
 };
 
 struct EnvMap

@@ -237,7 +237,8 @@ __global__ void __launch_bounds__(128) trace_fetch_wide_kernel(DevScene S, const
 
 int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void* out, bool any, int lights,
                         const float lo[3], const float hi[3], bool binning, uint32_t* keys, uint32_t* hist, int* perm,
-                        unsigned long long* next, uint32_t* status, cudaStream_t st)
+                        unsigned long long* next, uint32_t* status, cudaStream_t st, cudaEvent_t evStart,
+                        cudaEvent_t evStop)
 {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
@@ -264,17 +265,21 @@ int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void
         if (any)
         {
             per_sm = occupancy_blocks_per_sm((const void*)trace_fetch_wide_kernel<true>, 128);
+            if (evStart) cudaEventRecord(evStart, st);
             trace_fetch_wide_kernel<true><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
                 S, rays, order, n, nullptr, (uint8_t*)out, lights, next, status);
         }
         else
         {
             per_sm = occupancy_blocks_per_sm((const void*)trace_fetch_wide_kernel<false>, 128);
+            if (evStart) cudaEventRecord(evStart, st);
             trace_fetch_wide_kernel<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
                 S, rays, order, n, (int4*)out, nullptr, lights, next, status);
         }
+        if (evStop) cudaEventRecord(evStop, st);
         return (int)cudaGetLastError();
     }
+    if (evStart) cudaEventRecord(evStart, st);
     if (any)
     {
         per_sm = occupancy_blocks_per_sm((const void*)trace_persistent_kernel<true>, 128);
@@ -287,6 +292,7 @@ int launch_trace_binned(const DevScene& S, const float4* rays, long long n, void
         trace_persistent_kernel<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(
             S, rays, order, n, (int4*)out, nullptr, lights, next, status);
     }
+    if (evStop) cudaEventRecord(evStop, st);
     return (int)cudaGetLastError();
 }
 

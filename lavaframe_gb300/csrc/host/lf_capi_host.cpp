@@ -72,18 +72,37 @@ void push_quad(std::vector<Vec4>& v, std::vector<Vec4>& n, lfc::v3 a, lfc::v3 b,
     push_tri(v, n, a, c, d);
 }
 
-// Axis-aligned box [lo, hi] with outward normals (12 triangles).
-void push_box(std::vector<Vec4>& v, std::vector<Vec4>& n, lfc::v3 lo, lfc::v3 hi)
+// Quad a-b-c-d split into k x k quads (2 triangles each); k = 1 is push_quad itself. Grid
+// points interpolate the corners with weights (1 - t, t), which reproduce the corners exactly.
+void push_quad_grid(std::vector<Vec4>& v, std::vector<Vec4>& n, lfc::v3 a, lfc::v3 b, lfc::v3 c, lfc::v3 d, int k)
+{
+    using lfc::v3;
+    if (k <= 1)
+    {
+        push_quad(v, n, a, b, c, d);
+        return;
+    }
+    auto lerp = [](v3 x, v3 y, float t) { return x * (1.0f - t) + y * t; };
+    auto at = [&](int i, int j) {
+        const float u = (float)i / (float)k, w = (float)j / (float)k;
+        return lerp(lerp(a, b, u), lerp(d, c, u), w);
+    };
+    for (int j = 0; j < k; ++j)
+        for (int i = 0; i < k; ++i) push_quad(v, n, at(i, j), at(i + 1, j), at(i + 1, j + 1), at(i, j + 1));
+}
+
+// Axis-aligned box [lo, hi] with outward normals (12 triangles, or 12 k^2 with k x k faces).
+void push_box(std::vector<Vec4>& v, std::vector<Vec4>& n, lfc::v3 lo, lfc::v3 hi, int k = 1)
 {
     using lfc::v3;
     v3 p000(lo.x, lo.y, lo.z), p100(hi.x, lo.y, lo.z), p010(lo.x, hi.y, lo.z), p110(hi.x, hi.y, lo.z);
     v3 p001(lo.x, lo.y, hi.z), p101(hi.x, lo.y, hi.z), p011(lo.x, hi.y, hi.z), p111(hi.x, hi.y, hi.z);
-    push_quad(v, n, p000, p010, p110, p100);   // -z
-    push_quad(v, n, p001, p101, p111, p011);   // +z
-    push_quad(v, n, p000, p001, p011, p010);   // -x
-    push_quad(v, n, p100, p110, p111, p101);   // +x
-    push_quad(v, n, p000, p100, p101, p001);   // -y
-    push_quad(v, n, p010, p011, p111, p110);   // +y
+    push_quad_grid(v, n, p000, p010, p110, p100, k);   // -z
+    push_quad_grid(v, n, p001, p101, p111, p011, k);   // +z
+    push_quad_grid(v, n, p000, p001, p011, p010, k);   // -x
+    push_quad_grid(v, n, p100, p110, p111, p101, k);   // +x
+    push_quad_grid(v, n, p000, p100, p101, p001, k);   // -y
+    push_quad_grid(v, n, p010, p011, p111, p110, k);   // +y
 }
 
 Mat4 rigid_y(float angleDeg, lfc::v3 t)
@@ -432,10 +451,12 @@ lf_status lf_hscene_render_params(const lf_hscene* s, lf_render_params* p)
 // Procedural Cornell box: 1 m box open at z = 0, tall box 0.3x0.6x0.3 at 15 degrees,
 // short box 0.3x0.3x0.3 at -18 degrees, 0.25 m quad light 1 mm below the ceiling with
 // radiance (17, 12, 4), diffuse Disney materials, pinhole 45 degrees, depth 4, RR on.
-lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height)
+// subdiv > 1 splits every wall and box face into subdiv x subdiv quads (34 subdiv^2
+// triangles; the same surfaces), so the scene can be scaled for the serving mix.
+lf_status lf_gen_cornell_tess(lf_hscene* s, int32_t width, int32_t height, int32_t subdiv)
 {
     using lfc::v3;
-    if (!s || width <= 0 || height <= 0) return LF_ERR_INVALID;
+    if (!s || width <= 0 || height <= 0 || subdiv < 1 || subdiv > 4096) return LF_ERR_INVALID;
     Scene& sc = s->scene;
     if (sc.materials.empty()) sc.AddMaterial(Material());   // default material 0, as the loader
     int white = sc.AddMaterial(diffuse(0.73f, 0.73f, 0.73f));
@@ -457,19 +478,19 @@ lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height)
     for (const Wall& w : walls)
     {
         std::vector<Vec4> v, n;
-        push_quad(v, n, w.a, w.b, w.c, w.d);
+        push_quad_grid(v, n, w.a, w.b, w.c, w.d, subdiv);
         int mid = sc.AddMeshData("wall", v.data(), n.data(), (int)v.size());
         sc.AddMeshInstance(MeshInstance("wall", mid, Mat4(), w.mat));
     }
     {
         std::vector<Vec4> v, n;
-        push_box(v, n, v3(-0.15f, -0.3f, -0.15f), v3(0.15f, 0.3f, 0.15f));
+        push_box(v, n, v3(-0.15f, -0.3f, -0.15f), v3(0.15f, 0.3f, 0.15f), subdiv);
         int mid = sc.AddMeshData("tallbox", v.data(), n.data(), (int)v.size());
         sc.AddMeshInstance(MeshInstance("tallbox", mid, rigid_y(15.0f, v3(0.66f, 0.3f, 0.66f)), white));
     }
     {
         std::vector<Vec4> v, n;
-        push_box(v, n, v3(-0.15f, -0.15f, -0.15f), v3(0.15f, 0.15f, 0.15f));
+        push_box(v, n, v3(-0.15f, -0.15f, -0.15f), v3(0.15f, 0.15f, 0.15f), subdiv);
         int mid = sc.AddMeshData("shortbox", v.data(), n.data(), (int)v.size());
         sc.AddMeshInstance(MeshInstance("shortbox", mid, rigid_y(-18.0f, v3(0.33f, 0.15f, 0.35f)), white));
     }
@@ -490,6 +511,11 @@ lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height)
     s->options.tileWidth = width;
     s->options.tileHeight = height;
     return LF_OK;
+}
+
+lf_status lf_gen_cornell(lf_hscene* s, int32_t width, int32_t height)
+{
+    return lf_gen_cornell_tess(s, width, height, 1);
 }
 
 // Intersection microbench: `instances` meshes of `tris` random triangles each; every mesh

@@ -76,6 +76,35 @@ def test_small_pool_regenerates_and_matches_oracle(ctx):
                              shade_threads_per_sm=DEFAULT_SHADE_CAP)
 
 
+@pytest.mark.parametrize("slots", [1024, 4096])
+def test_sort_by_material_keeps_results(ctx, slots):
+    """Shade taking the surface hits bucketed by material class (opaque, metal, transmissive,
+    textured): per-path radiance, accumulation and ray counts unchanged. Pools smaller than the
+    frame's paths keep the step kernels (not only the drain) running."""
+    s = icospheres()
+    classes = set()
+    a = s.arrays()
+    _, _, inst_mat = s.layout()
+    for m in inst_mat:
+        mp = a["materials"][m]
+        classes.add(2 if mp[16] > 0 else 1 if mp[8] >= 0.5 else 0)
+    assert len(classes) >= 2
+    try:
+        ctx.configure_engine(slots=slots)
+        base, p = render(ctx, s, 3, size=(64, 36))
+        ctx.set_engine_sort(True)
+        got, _ = render(ctx, s, 3, size=(64, 36))
+    finally:
+        ctx.set_engine_sort(False)
+        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
+                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
+    assert same_bits(got["paths"], base["paths"])
+    assert same_bits(got["accum"], base["accum"])
+    assert got["counters"][1:] == base["counters"][1:]
+    ref_acc, _, _ = oracle.render(s.view(), p, 0, 3, want_paths=False)
+    assert same_bits(got["accum"], ref_acc)
+
+
 @pytest.mark.parametrize("blocks", [(64, 256, 96), (256, 64, 512)])
 def test_engine_block_sizes_do_not_change_results(ctx, blocks):
     s = scenes.build("cornell")
@@ -126,12 +155,11 @@ def test_autotuner_picks_a_setting_and_results_stay_exact(ctx, tmp_path):
     try:
         cache = tmp_path / "tune.json"
         r = autotune.tune(ctx, ds, p, spp=2, repeats=1, triangles=int(s.view().num_tris), cache=cache)
-        assert set(r["config"]) == set(autotune.DEFAULT) and len(r["trials"]) >= 10 and not r["cached"]
+        assert set(r["config"]) == set(autotune.DEFAULT) and len(r["trials"]) >= 11 and not r["cached"]
         again = autotune.tune(ctx, ds, p, spp=2, repeats=1, triangles=int(s.view().num_tris), cache=cache)
         assert again["cached"] and again["config"] == r["config"]
         got, _ = render(ctx, s, 2)
     finally:
         ds.close()
-        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
-                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
+        autotune.apply_default(ctx)
     assert same_bits(got["paths"], base["paths"])

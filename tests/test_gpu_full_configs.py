@@ -145,3 +145,31 @@ def test_c4_room_full_config(ctx):
            accum_rows_identical=dev_acc.tobytes() == ref_acc.tobytes(), oracle_s=t_cpu)
     assert bad == 0 or rel <= PATH_RTOL
     assert dev_acc.tobytes() == ref_acc.tobytes() or bad > 0
+
+
+def test_c1_image_rmse_against_16k_oracle_render(ctx):
+    """Image error of the GPU's Cornell renders against the FP64-accumulated 16,384-spp render
+    of the CPU oracle (tests/golden/make_c1_reference.py, samples disjoint from these): the
+    64-spp image's RMSE is stated, and 1024 spp must bring it down by about sqrt(16)."""
+    from tests.conftest import ROOT
+
+    gold = np.load(ROOT / "tests" / "golden" / "c1_reference_16k.npz")
+    ref = gold["mean"].astype(np.float64)
+    s = lf.HostScene().gen_cornell(256, 256).build()
+    p = s.render_params()
+    ds = ctx.upload(s)
+    f = lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM)
+    f.render(0, 64)
+    f.sync()
+    img64 = f.accum64() / 64
+    f.render(64, 1024 - 64)
+    f.sync()
+    img1024 = f.accum64() / 1024
+    f.close()
+    ds.close()
+    rmse64 = float(np.sqrt(((img64 - ref) ** 2).mean()))
+    rmse1024 = float(np.sqrt(((img1024 - ref) ** 2).mean()))
+    report("c1_rmse_vs_16k_fp64_oracle", rmse_64spp=rmse64, rmse_1024spp=rmse1024,
+           reference_spp=int(gold["spp"]), reference_mean=float(ref.mean()), image_mean_64spp=float(img64.mean()))
+    assert abs(img64.mean() - ref.mean()) < 0.02 * ref.mean()
+    assert rmse1024 < rmse64 / 3.0
