@@ -6,9 +6,17 @@ triangle soup of 2^20 instances x 10 triangles built with the reference's BVH al
   value   Grays/s with rays and hits resident in HBM (CUDA events on the launching stream)
   e2e     the same through lf_trace_closest with page-locked host buffers: every step copies
           the rays in and the hits out
+Roofline: the traversal kernel is bound by instruction issue under divergence, not by HBM
+(its DRAM traffic is a few percent of peak), so `roofline` is its warp-instruction issue rate
+(instructions per ray from the committed ncu summary x rays per second of the kernel alone,
+timed with CUDA events around each launch) against 4 issue slots per SM per clock at the SM
+clock sampled during the run; its DRAM bytes and their fraction of the measured HBM peak are
+reported beside it.
 Secondary numbers (reported under "extra"): progressive renders of the Cornell box
-(256^2, 64 spp, depth 4) and of the 13-icosphere ~1.06M-triangle scene (1920x1080,
-16 spp, depth 8) in Msamples/s and extension rays/s.
+(256^2, 64 spp, depth 4; image RMSE against the 16k-spp FP64 oracle render), of the
+13-icosphere ~1.06M-triangle scene and of the 64-icosphere 5.2M-triangle scene (1920x1080,
+16 spp, depth 8) in Msamples/s and extension rays/s, guided vs plain time to the plain
+1024-spp error on the occluded-light room at 1280x720, and the serving loop.
 
 `--impl reference` times the CPU restatement of the reference traversal (the reference's
 own GPU path is an OpenGL shader and cannot run here) on the host cores.
@@ -51,11 +59,12 @@ def parse():
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768/1024; 0 = 512)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
+    ap.add_argument("--sort-by-material", action="store_true", help="render workloads: engine sort-by-material")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
     ap.add_argument("--render-size", default="", help="c1/c3 workloads: override the resolution WxH (profiling)")
-    ap.add_argument("--c4-ref-spp", type=int, default=4096, help="guiding workload reference samples")
+    ap.add_argument("--c4-ref-spp", type=int, default=16384, help="guiding workload reference samples")
     ap.add_argument("--c4-alpha", type=float, default=0.5, help="guiding workload: mixture selection probability")
     ap.add_argument("--c4-every", type=int, default=2, help="guiding workload: train after every n-th batch")
     ap.add_argument("--c4-batch", type=int, default=16, help="guiding workload: samples per batch")
@@ -178,6 +187,26 @@ def soup_rays(s, n):
     return lf.gen_rays(root[0:3], root[3:6], n, 2), root
 
 
+PROFILE_KEYS = ("warp_inst_per_ray", "lanes_per_inst", "dram_bytes_per_ray", "l2_bytes_per_ray")
+
+
+def traversal_profile():
+    """Per-ray counters of the traversal kernel from the committed ncu summaries (the
+    full-scene capture first, then the reduced one): warp instructions, active lanes per
+    instruction, DRAM and L2 bytes."""
+    vals = {}
+    for name in ("c2_trace_wide_full.md", "c2_trace_wide_small.md"):
+        prof = ROOT / "profiles" / name
+        if not prof.exists():
+            continue
+        for line in prof.read_text().splitlines():
+            for key in PROFILE_KEYS:
+                if line.startswith(key + ":") and key not in vals:
+                    vals[key] = float(line.split(":")[1].split()[0])
+                    vals[key + "_from"] = f"profiles/{name}"
+    return vals
+
+
 def algorithmic_bytes_per_ray(stats, nrays):
     """Reference data model: 32 B ray + 16 B hit, 36 B per node box tested (two per inner
     node visit), 60 B per triangle test (12 B indices + 3 x 16 B vertices), 64 B per
@@ -249,7 +278,17 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True, size=None):
+def c1_reference_image():
+    """The Cornell box's 16,384-spp FP64-accumulated oracle render (a committed fixture made by
+    tests/golden/make_c1_reference.py), or None."""
+    path = ROOT / "tests" / "golden" / "c1_reference_16k.npz"
+    if not path.exists():
+        return None
+    g = np.load(path)
+    return g["mean"].astype(np.float64), int(g["spp"])
+
+
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True, size=None, sort=False):
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -268,6 +307,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
         from lavaframe_gb300 import autotune
 
         tuned = autotune.tune(ctx, ds, p, spp=spp, triangles=int(s.view().num_tris))
+    if sort:
+        ctx.set_engine_sort(True)
     f = lf.Frame(ctx, ds, p, flags)
     if spp_batch:
         f.set_batch(spp_batch)
@@ -282,70 +323,95 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
     out = {"Msamples_per_s": ctr[0] / (ms / 1e3) / 1e6, "ext_rays_per_s": ctr[1] / (ms / 1e3),
            "shadow_rays_per_s": ctr[2] / (ms / 1e3), "ms": ms, "spp": spp,
            "resolution": [p.width, p.height], "max_depth": p.max_depth,
-           "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1])}
+           "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1]), "sort_by_material": bool(sort)}
+    if which == "c1" and not size:
+        ref = c1_reference_image()
+        if ref is not None:
+            img = f.accum().astype(np.float64) / spp
+            out["rmse_vs_oracle_16k_fp64"] = float(np.sqrt(((img - ref[0]) ** 2).mean()))
+            out["oracle_reference_spp"] = ref[1]
     if tuned:
         out["autotuned"] = {"config": tuned["config"], "trials": len(tuned["trials"])}
     f.close()
+    if sort:
+        ctx.set_engine_sort(False)
     ds.close()
     return out
 
 
 SERVE_RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080), (2048, 2048)]
+SERVE_SIZES = [1e4, 1e5, 1e6, 5e6]   # triangles: the log-uniform range's ends and two points between
 
 
 def serve_scene_pool():
-    """Scenes the serving jobs draw from: the icosphere and room generators at sizes spread
-    log-uniformly over 10k-5M triangles (the Cornell generator has a fixed 34 triangles and
-    does not scale). Built once on the host; the server uploads them on admission."""
+    """Scenes the serving jobs draw from: each of the three generators (Cornell box with
+    tessellated faces, icospheres with the HDR environment, occluded-light room) at about 10k,
+    100k, 1M and 5M triangles. Built once on the host; the server uploads them on admission and
+    evicts idle ones least recently used first."""
     import lavaframe_gb300 as lf
 
     pool = []
-    for inst, level in ((1, 5), (4, 6), (13, 6), (64, 6)):           # 20k, 330k, 1.06M, 5.2M tris
+    for t in SERVE_SIZES:
+        k = max(1, int(round((t / 34.0) ** 0.5)))                      # 34 k^2 triangles
+        pool.append(("cornell", lf.HostScene().gen_cornell(256, 256, k).build()))
+    for inst, level in ((2, 4), (5, 5), (13, 6), (64, 6)):            # 10k, 102k, 1.06M, 5.2M
         pool.append(("icospheres", lf.HostScene().gen_icospheres(inst, level, 3, 1024, 512).build()))
-    for boxes in (1000, 16700):                                      # 12k, 200k tris
-        pool.append(("room", lf.HostScene().gen_room(boxes, 4).build()))
+    for t in SERVE_SIZES:
+        pool.append(("room", lf.HostScene().gen_room(int(t / 12), 4).build()))   # 12 triangles per box
     return pool
 
 
 def serve_jobs(pool, n, seed=11, max_spp=256):
-    """Job list: generator uniform, size log-uniform in [1e4, 5e6] triangles (nearest scene of
-    that generator), resolution, spp U{1..max_spp}, depth U{4..10}, Poisson arrival gaps of
-    rate 20 jobs/s."""
+    """Job list: generator uniform over the three, size log-uniform in [1e4, 5e6] triangles
+    (the pool scene of that generator nearest in log size), resolution, spp U{1..max_spp},
+    depth U{4..10}, and an exponential arrival gap of mean 1 (scaled by the rate later)."""
     rng = np.random.default_rng(seed)
     jobs = []
     for _ in range(n):
-        gen = ["icospheres", "room"][rng.integers(2)]
+        gen = ["cornell", "icospheres", "room"][rng.integers(3)]
         target = np.exp(rng.uniform(np.log(1e4), np.log(5e6)))
         cands = [(abs(np.log(max(1, int(sc.view().num_tris))) - np.log(target)), k) for k, (g, sc) in enumerate(pool)
                  if g == gen]
         scene = min(cands)[1]
         w, h = SERVE_RESOLUTIONS[rng.integers(len(SERVE_RESOLUTIONS))]
         jobs.append({"scene": scene, "width": w, "height": h, "spp": int(rng.integers(1, max_spp + 1)),
-                     "depth": int(rng.integers(4, 11)), "gap_s": float(rng.exponential(1.0 / 20.0))})
+                     "depth": int(rng.integers(4, 11)), "gap": float(rng.exponential(1.0))})
     return jobs
 
 
-def run_serving(ctx, n_jobs, max_spp=256):
-    """Serving loop workload: Poisson arrivals into lf_server, then the same jobs submitted at
-    once (batch-only). Returns latency percentiles and throughputs."""
+def run_serving(ctx, n_jobs, max_spp=256, budget_gb=0.0, rate=20.0, low_load=0.5):
+    """Serving loop workload. The same jobs run three ways: all submitted at once (batch-only
+    throughput), arriving as a Poisson stream at `rate` jobs/s, and arriving at the rate that
+    offers `low_load` of the batch throughput (so that latency is not queueing). A memory
+    budget below the scenes' total (budget_gb above the engine pool) makes the server evict
+    idle scenes under load."""
     import lavaframe_gb300 as lf
+    from lavaframe_gb300 import autotune
 
+    autotune.apply_default(ctx)   # creates the engine if needed, default setting
     pool = serve_scene_pool()
     jobs = serve_jobs(pool, n_jobs, max_spp=max_spp)
+    samples = int(sum(j["width"] * j["height"] * j["spp"] for j in jobs))
+    pool_bytes = ctx.engine_info()["device_bytes"]
+    budget = int(pool_bytes + budget_gb * (1 << 30)) if budget_gb > 0 else 0
 
     def params(j):
         p = pool[j["scene"]][1].render_params()
         p.width, p.height, p.max_depth = j["width"], j["height"], j["depth"]
         return p
 
-    def one_run(arrivals):
-        srv = lf.Server(ctx)
+    def one_run(arrival_rate):
+        srv = lf.Server(ctx, memory_budget=budget)
         sids = [srv.add_scene(sc) for _, sc in pool]
         t0 = time.perf_counter()
         ids = []
+        due = 0.0
         for j in jobs:
-            if arrivals:
-                time.sleep(j["gap_s"])
+            if arrival_rate:
+                due += j["gap"] / arrival_rate
+                wait = due - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
             ids.append(srv.submit(sids[j["scene"]], params(j), j["spp"]))
         for jid in ids:
             srv.wait(jid)
@@ -356,19 +422,23 @@ def run_serving(ctx, n_jobs, max_spp=256):
             srv.release(jid)
         srv.close()
         lat = np.array([i["finish_ms"] - i["submit_ms"] for i in infos])
-        samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
         span = (max(i["finish_ms"] for i in infos) - min(i["submit_ms"] for i in infos)) / 1e3
-        return {"wall_s": wall, "makespan_s": span, "Msamples_per_s": samples / span / 1e6,
-                "ext_rays_per_s": st["ext_rays"] / span, "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
-                "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"]}
+        return {"arrival_rate_per_s": arrival_rate or None, "wall_s": wall, "makespan_s": span,
+                "Msamples_per_s": samples / span / 1e6, "ext_rays_per_s": st["ext_rays"] / span,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "max_ms": float(lat.max()), "scene_uploads": st["scene_uploads"],
+                "scene_evictions": st["scene_evictions"]}
 
-    serve = one_run(True)
-    batch = one_run(False)
-    return {"jobs": n_jobs, "samples": int(sum(j["width"] * j["height"] * j["spp"] for j in jobs)),
-            "arrival_rate_per_s": 20, "serving": serve, "batch_only": batch,
+    batch = one_run(0.0)
+    serve = one_run(rate)
+    low_rate = low_load * n_jobs / batch["makespan_s"]
+    low = one_run(low_rate)
+    return {"jobs": n_jobs, "samples": samples, "max_spp": max_spp, "memory_budget_bytes": budget or None,
+            "engine_pool_bytes": pool_bytes, "batch_only": batch, "serving": serve,
             "serving_over_batch": serve["Msamples_per_s"] / batch["Msamples_per_s"],
-            "scenes": [{"generator": g, "triangles": int(sc.view().num_tris)} for g, sc in pool]}
+            "serving_low_load": dict(low, offered_load=low_load),
+            "scenes": [{"generator": g, "triangles": int(sc.view().num_tris), "device_bytes": None}
+                       for g, sc in pool]}
 
 
 def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, max_factor=3.0, alpha=0.5, lr=1e-2):
@@ -466,7 +536,7 @@ def main():
         ctx.close()
         return
     if args.workload == "c5":
-        r = run_serving(ctx, args.jobs or 48)
+        r = run_serving(ctx, args.jobs or 48, budget_gb=3.0)
         if rank == 0:
             print(json.dumps({"metric": "c5 serving Msamples/s", "value": r["serving"]["Msamples_per_s"],
                               "unit": "Msamples/s", "detail": r}), flush=True)
@@ -475,7 +545,7 @@ def main():
     if args.workload != "microbench":
         size = tuple(int(x) for x in args.render_size.split("x")) if args.render_size else None
         r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags,
-                         tune=args.autotune, wide=args.traversal == "wide", size=size)
+                         tune=args.autotune, wide=args.traversal == "wide", size=size, sort=args.sort_by_material)
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)
@@ -499,12 +569,15 @@ def main():
         ctx._c(L.lf_trace_closest_device(ctx.h, ds.h, d_rays, nrays, d_hits, 0))
     ctx.sync()
     barrier(world)
+    ctx.kernel_timer(True)        # event pair around each traversal kernel launch
     with ClockSampler(local) as clk:
         ctx.timer_start()
         for _ in range(args.steps):
             ctx._c(L.lf_trace_closest_device(ctx.h, ds.h, d_rays, nrays, d_hits, 0))
         ms = ctx.timer_stop()
         ctx.sync()
+    kernel_ms, kernel_launches = ctx.kernel_timer_read()
+    ctx.kernel_timer(False)
     barrier(world)
     ms = max_over_ranks(world, ms)
     value = world * nrays * args.steps / (ms / 1e3) / 1e9
@@ -545,29 +618,53 @@ def main():
         ref_hits, _ = oracle.trace_closest(s.view(), rays[:4096], cull_rel=1e-4, cull_abs=cull_abs)
         extra["parity_spot_check_4096_rays"] = bool(ref_hits.tobytes() == hits[:4096].tobytes())
         bpr = algorithmic_bytes_per_ray(ostats, sample)
-        peak, peak_kind = measured_peaks()
-        launch_s = ms / 1e3 / args.steps
-        achieved = bpr * nrays / launch_s / 1e9
-        # DRAM bytes per ray from the committed ncu summary of the traversal kernel (a reduced case
-        # captured under the size rule), scaled to this launch by its ray count
-        prof = ROOT / "profiles" / "c2_trace_wide_small.md"
-        traffic = None
-        if prof.exists():
-            for line in prof.read_text().splitlines():
-                if line.startswith("dram_bytes_per_ray:"):
-                    traffic = float(line.split(":")[1].split()[0]) * nrays
+        hbm_peak, peak_kind = measured_peaks()
+        # the traversal kernel alone: CUDA events around each of its launches in the timed loop
+        kernel_s = kernel_ms / 1e3 / max(1, kernel_launches)
+        kernel_rays_per_s = nrays / kernel_s
+        # issue roofline: 4 warp schedulers per SM, one instruction each per clock, at the median
+        # SM clock sampled during the timed region; instructions per ray from the ncu summary
+        attrs = ctx.device_attrs()
+        clocks = clk.summary()
+        sm_mhz = clocks.get("sm_mhz") or attrs["max_sm_mhz"]
+        prof = traversal_profile()
+        issue_peak = attrs["sm_count"] * 4 * sm_mhz * 1e6 / 1e9
+        inst = prof.get("warp_inst_per_ray")
+        achieved = inst * kernel_rays_per_s / 1e9 if inst else None
+        traffic = prof["dram_bytes_per_ray"] * nrays if "dram_bytes_per_ray" in prof else None
+        dram_gbs = traffic / kernel_s / 1e9 if traffic else None
+        roofline = {
+            "bound": "issue", "achieved": achieved, "peak": issue_peak, "unit": "Gwarp-instructions/s",
+            "frac": achieved / issue_peak if achieved else None, "traffic": traffic,
+            "peak_kind": f"{attrs['sm_count']} SMs x 4 schedulers x {sm_mhz:.0f} MHz (median SM clock sampled "
+                         f"during the timed region)",
+            "kernel": "trace_fetch_wide_kernel<false>", "kernel_ms_per_launch": kernel_s * 1e3,
+            "kernel_launches": kernel_launches, "kernel_rays_per_s": kernel_rays_per_s,
+            "warp_inst_per_ray": inst, "lanes_per_inst": prof.get("lanes_per_inst"),
+            "simt_efficiency": prof["lanes_per_inst"] / 32.0 if "lanes_per_inst" in prof else None,
+            "counters_from": prof.get("warp_inst_per_ray_from"),
+            "dram_bytes_per_ray": prof.get("dram_bytes_per_ray"), "dram_GBps": dram_gbs,
+            "dram_frac_of_hbm": dram_gbs / hbm_peak if dram_gbs else None,
+            "l2_bytes_per_ray": prof.get("l2_bytes_per_ray"),
+            "hbm_peak_GBps": hbm_peak, "hbm_peak_kind": peak_kind,
+            "reference_model_bytes_per_ray": bpr,
+            "note": "instruction issue is the bound (DRAM traffic is a few percent of HBM); the reference "
+                    "data-model bytes (every binary node box, triangle and transform the reference shader would "
+                    "fetch) are informational"}
         if not args.no_extras:
-            for w, flags in (("c1", 0), ("c3_1m", 0), ("c3_1m_per_batch", 8), ("c3_1m_autotuned", 0)):
-                try:
-                    extra[w] = render_extra(ctx, "c1" if w == "c1" else "c3", flags=flags,
-                                            tune=(w == "c3_1m_autotuned"))
-                except Exception as e:  # reported, not fatal for the headline
-                    extra[w] = {"error": str(e)}
             from lavaframe_gb300 import autotune
 
-            autotune.apply_default(ctx)   # the remaining workloads run on the default engine
-            for w, fn in (("c4_guiding_640x360", lambda: run_guiding(ctx, 640, 360, 4096)),
-                          ("c5_serving_16_jobs", lambda: run_serving(ctx, 16, max_spp=64))):
+            renders = (("c1", "c1", {}), ("c3_1m", "c3", {}), ("c3_1m_sort_by_material", "c3", {"sort": True}),
+                       ("c3_1m_per_batch", "c3", {"flags": 8}), ("c3_5m", "c3full", {}),
+                       ("c3_1m_autotuned", "c3", {"tune": True}))
+            for w, which, kw in renders:
+                try:
+                    extra[w] = render_extra(ctx, which, **kw)
+                except Exception as e:  # reported, not fatal for the headline
+                    extra[w] = {"error": str(e)}
+                autotune.apply_default(ctx)   # the other workloads run on the default engine
+            for w, fn in (("c4_guiding_1280x720", lambda: run_guiding(ctx, 1280, 720, args.c4_ref_spp)),
+                          ("c5_serving_48_jobs", lambda: run_serving(ctx, 48, budget_gb=3.0))):
                 try:
                     extra[w] = fn()
                 except Exception as e:  # reported, not fatal for the headline
@@ -587,12 +684,10 @@ def main():
                        "l2": "inputs larger than L2 (rays 512 MiB + scene > 129 MB), no flush"},
             "e2e": {"value": e2e, "unit": "Grays/s", "h2d_bytes_per_step": int(rays.nbytes),
                     "d2h_bytes_per_step": int(nrays * 16)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": peak_kind,
-                         "note": "algorithmic bytes of the reference data model per launch / CUDA-event launch time"},
+            "roofline": roofline,
             "cpu_baseline": {"value": cpu_v, "unit": "Grays/s", "cores": cores, "kind": "port",
                              "sample": f"{sample} of the 2^{args.rays_log2} rays, {cpu_dt:.1f} s"},
-            "clocks": clk.summary(),
+            "clocks": clocks,
             # per binned query: ray_keys, the three bin-scan kernels, ray_scatter, traversal
             "gpu_launches": args.steps * 6,
             "extra": extra,

@@ -128,6 +128,7 @@ _SIG = {
     "lf_guide_train": (C.c_int, [_P, _F, C.c_int32, C.c_float, _F]),
     "lf_guide_train_device": (C.c_int, [_P, _P, C.c_int32, C.c_float]),
     "lf_guide_eval": (C.c_int, [_P, _F, C.c_int32, _F, _F]),
+    "lf_guide_set_tensor_path": (C.c_int, [_P, C.c_int32]),
     "lf_frame_set_guide": (C.c_int, [_P, _P, C.c_float, C.c_int32, C.c_float]),
     "lf_frame_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 }
@@ -618,6 +619,10 @@ class Guide:
         loss = np.zeros(1, np.float32)
         self.ctx._c(lib().lf_guide_train(self.h, _fp(samples), len(samples), lr, _fp(loss)))
         return float(loss[0])
+
+    def set_tensor_path(self, tcgen05):
+        """MLP inference on the tcgen05 tensor cores (True) or the warp-level mma.sync kernel."""
+        self.ctx._c(lib().lf_guide_set_tensor_path(self.h, 1 if tcgen05 else 0))
 
     def eval(self, queries):
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, GUIDE_SAMPLE_FLOATS)

@@ -566,6 +566,7 @@ struct lf_guide
     Net net{};
     int step = 0;
     float lr = 1e-2f;
+    int tensorPath = 0;             // inference on tcgen05 (1) or warp-level mma.sync (0)
 };
 
 namespace guidehost
@@ -617,6 +618,7 @@ using namespace guidehost;
 namespace lfrt
 {
 lfd::guide::Net guide_net(const lf_guide* g) { return g->net; }
+int guide_tensor_path(const lf_guide* g) { return g->tensorPath; }
 }
 
 extern "C" {
@@ -805,6 +807,14 @@ lf_status lf_guide_train(lf_guide* gd, const float* samples, int32_t n, float lr
     return check_device(c);
 }
 
+lf_status lf_guide_set_tensor_path(lf_guide* gd, int32_t tcgen05)
+{
+    if (!gd || tcgen05 < 0 || tcgen05 > 1) return LF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(gd->ctx->mu);
+    gd->tensorPath = tcgen05;
+    return LF_OK;
+}
+
 lf_status lf_guide_eval(lf_guide* gd, const float* queries, int32_t n, float* mix, float* pdf)
 {
     if (!gd || !queries || n <= 0 || (!mix && !pdf)) return LF_ERR_INVALID;
@@ -818,15 +828,9 @@ lf_status lf_guide_eval(lf_guide* gd, const float* queries, int32_t n, float* mi
     float* dmix = gd->scratch + qf;
     float* dpdf = dmix + (size_t)n * kMixFloats;
     cudaMemcpyAsync(dq, queries, qf * sizeof(float), cudaMemcpyHostToDevice, c->stream);
-    static bool attr = false;
-    if (!attr)
-    {
-        cudaFuncSetAttribute(guide_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem());
-        attr = true;
-    }
-    const int tiles = (n + 15) / 16;
-    guide_infer_kernel<<<std::max(1, std::min(4096, (tiles + kInferWarps - 1) / kInferWarps)), kInferWarps * 32,
-                         infer_smem(), c->stream>>>(gd->net, dq, n, nullptr, dmix);
+    const int ie = gd->tensorPath ? launch_infer_tc(gd->net, dq, nullptr, n, dmix, c->d_status, c->stream)
+                                  : launch_infer(gd->net, dq, nullptr, n, dmix, c->stream);
+    if (ie) return cuda_fail(c, (cudaError_t)ie, "guide inference launch");
     guide_pdf_kernel<<<grid_blocks(n, 256), 256, 0, c->stream>>>(dmix, dq, n, dpdf);
     if (mix) cudaMemcpyAsync(mix, dmix, (size_t)n * kMixFloats * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (pdf) cudaMemcpyAsync(pdf, dpdf, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream);

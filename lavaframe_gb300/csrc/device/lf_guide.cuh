@@ -129,6 +129,10 @@ __device__ __forceinline__ float mix_pdf(const float* mix, float wx, float wy, f
 // Mixture of every query record (16 floats: position, outgoing direction, normal, ...) into
 // mix (kMixFloats each); the count is read from nDev. Launched on `st`; returns a CUDA error.
 int launch_infer(const Net& net, const float* queries, const int* nDev, int cap, float* mix, cudaStream_t st);
+// The same on the tcgen05 tensor cores (lf_guide_tc.cu): tiles of 128 queries, accumulators in
+// TMEM. A bounded wait that runs out sets LF_DEVERR_GUIDE_TIMEOUT in `status`.
+int launch_infer_tc(const Net& net, const float* queries, const int* nDev, int cap, float* mix, uint32_t* status,
+                    cudaStream_t st);
 
 // Samples a direction from the compact mixture with uniforms u0 (lobe), u1, u2.
 __device__ __forceinline__ void mix_sample(const float* mix, float u0, float u1, float u2, float* wx, float* wy,

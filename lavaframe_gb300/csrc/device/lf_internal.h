@@ -20,6 +20,7 @@ namespace lfrt
 struct EngineHost;
 void engine_destroy(EngineHost* e);
 lfd::guide::Net guide_net(const lf_guide* g);
+int guide_tensor_path(const lf_guide* g);
 }
 
 struct lf_ctx

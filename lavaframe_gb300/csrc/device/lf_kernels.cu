@@ -424,7 +424,8 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
     extend_kernel<<<grid_for((const void*)extend_kernel, B, cap), B, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status,
                                                                               b.ctr);
     guide_query_kernel<<<grid_for((const void*)guide_query_kernel, B, cap), B, 0, st>>>(S, ps, qin, cin, g.queries);
-    int e = guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
+    int e = g.tensorPath ? guide::launch_infer_tc(g.net, g.queries, cin, (int)cap, g.mix, b.status, st)
+                         : guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
     if (e) return e;
     GuideCtx gc{g.mix, g.rec, g.alpha, g.maxDepth};
     shade_guided_kernel<<<grid_for((const void*)shade_guided_kernel, B, cap), B, 0, st>>>(

@@ -60,6 +60,7 @@ struct GuideBuffers
     float alpha;         // mixture selection probability
     int maxDepth;
     float weightClamp;   // training weights are clamped to this
+    int tensorPath;      // 1: MLP inference on tcgen05 (lf_guide_tc.cu), 0: warp-level mma.sync
 };
 
 int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps, const BounceBuffers& b,

@@ -1351,6 +1351,7 @@ lf_status run_batch(lf_frame* f, Params P, int firstSample, int n, bool record =
     {
         GuideBuffers gb = f->gb;
         gb.net = guide_net(f->guide);
+        gb.tensorPath = guide_tensor_path(f->guide);
         gb.rec = record ? f->gb.rec : nullptr;
         for (int b = 0; b < P.maxDepth && !e; ++b) e = launch_bounce_guided(Sv, P, f->ps, bb, gb, b, cap, c->stream);
         if (!e && record)

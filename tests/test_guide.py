@@ -137,3 +137,34 @@ def test_training_fits_a_position_dependent_distribution(ctx):
     # uniform density on the sphere: -log(1 / 4 pi) = 2.53
     assert first > 2.0
     assert last < first - 2.0, (first, last)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1000, 128 * 152 * 3 + 77])
+def test_tcgen05_inference_matches_warp_mma_and_oracle(ctx, n):
+    """MLP inference on the tcgen05 tensor cores (128-query tiles, TMEM accumulators) against
+    the warp-level mma.sync kernel and the FP64 oracle on the same FP16 parameters; the second
+    size runs several tiles per CTA and ends on a partial tile."""
+    grid, W = G.init_params(11)
+    grid = [g * 2e3 for g in grid]
+    W = [x * 3.0 for x in W]
+    wflat, gflat = flat_params(grid, W)
+    p, wo, nrm, wd, w = random_batch(n, 5)
+    rec = records(p, wo, nrm, wd, w)
+    gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1])
+    try:
+        gd.set_params(wflat, gflat)
+        mix_w, pdf_w = gd.eval(rec)
+        gd.set_tensor_path(True)
+        mix_t, pdf_t = gd.eval(rec)
+        assert ctx.device_errors() == 0
+    finally:
+        gd.close()
+    np.testing.assert_allclose(mix_t, mix_w, rtol=1e-2, atol=1e-3)
+    np.testing.assert_allclose(pdf_t, pdf_w, rtol=2e-2, atol=1e-4)
+    close = np.isclose(mix_t, mix_w, rtol=1e-5, atol=1e-6).mean()
+    assert close > 0.9, close     # most values agree to FP32 summation order
+    m = min(n, 2000)
+    x, _ = G.encode([G.f16(g) for g in grid], p[:m], wo[:m], nrm[:m])
+    _, out = G.forward([G.f16(v) for v in W], G.f16(x))
+    np.testing.assert_allclose(pdf_t[:m], G.pdf(out, wd[:m]), rtol=3e-2, atol=1e-4)
