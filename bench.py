@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--c4-every", type=int, default=2, help="guiding workload: train after every n-th batch")
     ap.add_argument("--c4-batch", type=int, default=16, help="guiding workload: samples per batch")
     ap.add_argument("--c4-lr", type=float, default=1e-2, help="guiding workload: Adam learning rate")
+    ap.add_argument("--c4-tensor", type=int, default=0, help="guiding workload: MLP inference on tcgen05 (1)")
     ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
@@ -441,7 +442,8 @@ def run_serving(ctx, n_jobs, max_spp=256, budget_gb=0.0, rate=20.0, low_load=0.5
                        for g, sc in pool]}
 
 
-def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, max_factor=3.0, alpha=0.5, lr=1e-2):
+def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, max_factor=3.0, alpha=0.5, lr=1e-2,
+                tensor=0):
     """Time-to-error of learned path guiding on the occluded-light room (16.7k boxes, ~200k
     triangles, depth 10): the plain tracer's error after plain_spp samples, against an FP64
     reference of ref_spp samples, and the wall time the guided tracer (trained online, Adam
@@ -483,6 +485,7 @@ def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, 
     f.close()
 
     g = lf.Guide(ctx, lo, hi, seed=1)
+    g.set_tensor_path(bool(tensor))
     f = frame()
     f.set_batch(batch)
     f.set_guide(g, alpha, every, lr)
@@ -507,7 +510,8 @@ def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, 
             "plain_rmse": target, "guided_reached": reached, "guided_spp": done, "guided_s": spent,
             "guided_rmse": last, "time_ratio": spent / t_plain if reached else None,
             "adam_steps": st["adam_steps"], "training_samples": st["training_samples"],
-            "batch": batch, "train_every": every, "alpha": alpha, "lr": lr}
+            "batch": batch, "train_every": every, "alpha": alpha, "lr": lr,
+            "mlp_inference": "tcgen05" if tensor else "mma.sync"}
 
 
 def main():
@@ -529,7 +533,7 @@ def main():
     if args.workload == "c4":
         cw, ch = (int(x) for x in args.c4_size.split("x"))
         r = run_guiding(ctx, cw, ch, args.c4_ref_spp, batch=args.c4_batch, every=args.c4_every, alpha=args.c4_alpha,
-                        lr=args.c4_lr)
+                        lr=args.c4_lr, tensor=args.c4_tensor)
         if rank == 0:
             print(json.dumps({"metric": "c4 guided / plain time to the plain 1024-spp error", "value": r["time_ratio"],
                               "unit": "ratio", "higher_is_better": False, "detail": r}), flush=True)
