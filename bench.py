@@ -216,18 +216,21 @@ def algorithmic_bytes_per_ray(stats, nrays):
     return 32.0 + 16.0 + (36.0 * 2.0 * inner + 60.0 * tris + 64.0 * inst) / nrays
 
 
-def cpu_baseline(view, rays, target_s, cull_abs):
+def cpu_baseline(view, rays, target_s):
+    """The oracle's ClosestHit with the shader's semantics (no distance culling: every box the
+    reference's traversal would test is tested) on all host threads, over a leading sample of
+    the rays sized to take about target_s seconds."""
     import oracle
 
     threads = os.cpu_count() or 1
-    n = min(len(rays), 1 << 16)
+    n = min(len(rays), 1 << 14)
     t = time.time()
-    _, st = oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    _, st = oracle.trace_closest(view, rays[:n], threads=threads)
     dt = max(time.time() - t, 1e-3)
     m = int(min(len(rays), max(n, n * target_s / dt)))
     m = max(n, (m // n) * n)
     t = time.time()
-    _, st = oracle.trace_closest(view, rays[:m], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    _, st = oracle.trace_closest(view, rays[:m], threads=threads)
     dt = time.time() - t
     return m / dt / 1e9, threads, m, dt, st
 
@@ -241,25 +244,26 @@ def run_reference(args, world, rank):
     from lavaframe_gb300 import build as b
     b.build_core()
     b.build_oracle()
+    # The scene and rays come from the product's host layer: the GPU host has no reference
+    # checkout, and the layer's node arrays are byte-identical to the reference's own build.
     s, _, _ = build_soup(args.instances_log2)
     rays, root = soup_rays(s, 1 << args.rays_log2)
-    extent = float(np.abs(root[:6]).max())
-    cull_abs = 64 * float(np.spacing(np.float32(extent)))
     view = s.view()
     threads = os.cpu_count() or 1
-    n = min(len(rays), 1 << 16)
+    # ClosestHit with the shader's semantics: no distance culling (closest_hit.glsl:69-201)
+    n = min(len(rays), 1 << 14)
     t = time.time()
-    oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+    oracle.trace_closest(view, rays[:n], threads=threads)
     per = (time.time() - t) / n
-    sample = int(min(len(rays), max(n, 6.0 / max(per, 1e-9))))
+    sample = int(min(len(rays), max(n, 5.0 / max(per, 1e-9))))
     sample = max(n, (sample // n) * n)
     for i in range(args.warmup):
-        oracle.trace_closest(view, rays[:n], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+        oracle.trace_closest(view, rays[:n], threads=threads)
     times = []
     for i in range(args.steps):
         off = (i * sample) % max(1, len(rays) - sample + 1)
         t = time.time()
-        oracle.trace_closest(view, rays[off:off + sample], cull_rel=1e-4, cull_abs=cull_abs, threads=threads)
+        oracle.trace_closest(view, rays[off:off + sample], threads=threads)
         times.append(time.time() - t)
     total = sum(times)
     v = sample * args.steps / total / 1e9
@@ -274,7 +278,9 @@ def run_reference(args, world, rank):
                          "sample": f"{sample} rays per step of the 2^{args.rays_log2}-ray set"},
         "e2e": {"value": v, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference traces in an OpenGL fragment shader that cannot run on this host; "
-                "this arm times the scalar C++ restatement of its traversal on all host cores",
+                "this arm times the scalar C++ restatement of its ClosestHit (shader semantics, no distance "
+                "culling) on all host cores; scene and rays are built by the product's host layer, whose node "
+                "arrays are byte-identical to the reference's build; each step is a sample of the 2^24 rays",
     }
     print(json.dumps(line), flush=True)
 
@@ -614,12 +620,9 @@ def main():
     if rank == 0:
         import oracle
 
-        extent = float(np.abs(root[:6]).max())
-        cull_abs = 64 * float(np.spacing(np.float32(extent)))
-        cpu_v, cores, sample, cpu_dt, ostats = cpu_baseline(s.view(), rays, 0.0 if args.no_cpu else args.cpu_seconds,
-                                                            cull_abs)
+        cpu_v, cores, sample, cpu_dt, ostats = cpu_baseline(s.view(), rays, 0.0 if args.no_cpu else args.cpu_seconds)
         # spot check: the sampled rays agree with the oracle bit for bit
-        ref_hits, _ = oracle.trace_closest(s.view(), rays[:4096], cull_rel=1e-4, cull_abs=cull_abs)
+        ref_hits, _ = oracle.trace_closest(s.view(), rays[:4096])
         extra["parity_spot_check_4096_rays"] = bool(ref_hits.tobytes() == hits[:4096].tobytes())
         bpr = algorithmic_bytes_per_ray(ostats, sample)
         hbm_peak, peak_kind = measured_peaks()

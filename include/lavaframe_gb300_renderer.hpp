@@ -14,6 +14,15 @@
 //  - a moved camera or edited instances reset the accumulation (TiledRenderer.cpp:471-484).
 // There is no GL: Present/SetViewport are no-ops returning 0, Denoise is not available
 // (the reference's OIDN binary is not part of this library) and returns 0.
+//
+// The base class is a template parameter. Inside the LavaFrame application it is the
+// reference's own abstract renderer, so the object drops into `GlobalState.renderer`
+// (a `LavaFrame::Renderer*`, GlobalState.h:7) unchanged:
+//     new LavaFrame::CudaRenderer<LavaFrame::Scene, LavaFrame::Renderer>(scene, 0)
+// The base is then constructed with (scene, "") and its GL state is never initialised
+// (its destructor releases GL objects only when initialised, Renderer.cpp:44-48). Without
+// the reference headers the default base is RendererInterface, the same virtuals without the
+// GL handles.
 #pragma once
 
 #include <cmath>
@@ -21,6 +30,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "lavaframe_gb300.h"
@@ -85,11 +95,30 @@ inline lf_scene_view MakeSceneView(const SceneT& sc)
     return v;
 }
 
-template <class SceneT>
-class CudaRenderer : public RendererInterface
+namespace detail
+{
+// Constructs the renderer base: (scene, shaders directory) for LavaFrame::Renderer
+// (Renderer.h:100), default construction for RendererInterface.
+template <class Base, class SceneT, bool = std::is_same<Base, RendererInterface>::value>
+struct RendererBase : Base
+{
+    explicit RendererBase(SceneT* scene) : Base(scene, std::string()) {}
+};
+template <class Base, class SceneT>
+struct RendererBase<Base, SceneT, true> : Base
+{
+    explicit RendererBase(SceneT*) {}
+};
+}
+
+template <class SceneT, class Base = RendererInterface>
+class CudaRenderer : public detail::RendererBase<Base, SceneT>
 {
 public:
-    CudaRenderer(SceneT* scene, int device = 0) : scene_(scene), device_(device) {}
+    CudaRenderer(SceneT* scene, int device = 0)
+        : detail::RendererBase<Base, SceneT>(scene), scene_(scene), device_(device)
+    {
+    }
     ~CudaRenderer() override { Finish(); }
 
     void Init() override

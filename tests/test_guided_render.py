@@ -68,3 +68,35 @@ def test_trained_guide_lowers_error_at_equal_samples(ctx):
     e_plain = np.sqrt(((plain - ref) ** 2).mean())
     e_guided = np.sqrt(((guided - ref) ** 2).mean())
     assert e_guided < 0.85 * e_plain, (e_plain, e_guided)
+
+
+@pytest.mark.parametrize("tensor", [False, True])
+def test_online_training_helps_for_every_seed(ctx, tensor):
+    """Online training as the guiding workload runs it (batches of 16 samples, Adam after every
+    second batch, lr 1e-2), repeated over four guide seeds and sample streams: every run's
+    guide must lower the error at equal samples, and the worst run is bounded. Inference on
+    the warp-level kernel and on tcgen05."""
+    s, lo, hi = room()
+    p = s.render_params()
+    p.width, p.height = 96, 54
+    ds = ctx.upload(s)
+    ratios = []
+    try:
+        ref, _ = render(ctx, ds, p, 0, 8192, batch=64)
+        plain, _ = render(ctx, ds, p, 90000, 64)
+        e_plain = np.sqrt(((plain - ref) ** 2).mean())
+        for seed in range(1, 5):
+            g = lf.Guide(ctx, lo, hi, seed=seed)
+            g.set_tensor_path(tensor)
+            try:
+                _, st = render(ctx, ds, p, 20000 * seed, 384, guide=g, train_every=2, batch=16)
+                guided, _ = render(ctx, ds, p, 90000, 64, guide=g, train_every=0)
+            finally:
+                g.close()
+            assert st["adam_steps"] > 0
+            ratios.append(float(np.sqrt(((guided - ref) ** 2).mean()) / e_plain))
+    finally:
+        ds.close()
+    assert max(ratios) < 0.95, ratios
+    assert np.mean(ratios) < 0.85, ratios
+    assert ctx.device_errors() == 0
