@@ -224,59 +224,6 @@ __device__ __forceinline__ void encode_tile(const Net& net, const float* p, cons
     }
 }
 
-// Loss of one sample and d loss / d outputs (without the 1/N of the mean), clamped to the
-// FP16 range. Mirrors oracle/guide.py loss_and_grads.
-__device__ __forceinline__ float sample_loss_grad(const float* out, const float dir[3], float weight, float* d_out)
-{
-    float mu[kLobes][3], kap[kLobes], f[kLobes], dot[kLobes], pi[kLobes], nrm[kLobes];
-    float mx = -1e30f;
-    for (int i = 0; i < kLobes; ++i) mx = fmaxf(mx, out[5 * i + 4]);
-    float es = 0.f;
-    for (int i = 0; i < kLobes; ++i)
-    {
-        pi[i] = __expf(out[5 * i + 4] - mx);
-        es += pi[i];
-    }
-    float q = 0.f;
-    for (int i = 0; i < kLobes; ++i)
-    {
-        pi[i] /= es;
-        const float* o = out + 5 * i;
-        nrm[i] = sqrtf(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + 1e-6f);
-        mu[i][0] = o[0] / nrm[i];
-        mu[i][1] = o[1] / nrm[i];
-        mu[i][2] = o[2] / nrm[i];
-        kap[i] = __expf(fminf(fmaxf(o[3], -3.f), 7.f));
-        dot[i] = mu[i][0] * dir[0] + mu[i][1] * dir[1] + mu[i][2] * dir[2];
-        f[i] = vmf_norm(kap[i]) * __expf(kap[i] * (dot[i] - 1.f));
-        q += pi[i] * f[i];
-    }
-    const float dq = -weight / (q + 1e-12f);
-    float gpi_avg = 0.f;
-    for (int i = 0; i < kLobes; ++i) gpi_avg += pi[i] * (dq * f[i]);
-    for (int i = 0; i < kLobes; ++i)
-    {
-        const float* o = out + 5 * i;
-        const float gpi = dq * f[i];
-        const float glg = pi[i] * (gpi - gpi_avg);
-        const float gf = dq * pi[i];
-        const float e2 = __expf(-2.f * kap[i]);
-        const float dlogf = 1.f / kap[i] - 2.f * e2 / (1.f - e2) + (dot[i] - 1.f);
-        const float gk = gf * f[i] * dlogf;
-        const float gkr = (o[3] > -3.f && o[3] < 7.f) ? gk * kap[i] : 0.f;
-        const float gm = gf * f[i] * kap[i];
-        const float gmx = gm * dir[0], gmy = gm * dir[1], gmz = gm * dir[2];
-        const float proj = gmx * mu[i][0] + gmy * mu[i][1] + gmz * mu[i][2];
-        float* d = d_out + 5 * i;
-        d[0] = (gmx - mu[i][0] * proj) / nrm[i];
-        d[1] = (gmy - mu[i][1] * proj) / nrm[i];
-        d[2] = (gmz - mu[i][2] * proj) / nrm[i];
-        d[3] = gkr;
-        d[4] = glg;
-    }
-    for (int k = 0; k < 40; ++k) d_out[k] = fminf(fmaxf(d_out[k], -60000.f), 60000.f);
-    return -weight * __logf(q + 1e-12f);
-}
 }
 
 // One pass over n training samples: adds the per-sample gradients (not divided by n) of every
@@ -594,6 +541,12 @@ int grid_blocks(int n, int b) { return std::min(4096, std::max(1, (n + b - 1) / 
 lf_status run_gradients(lf_guide* gd, const float* d_samples, int n)
 {
     lf_ctx* c = gd->ctx;
+    if (gd->tensorPath)
+    {
+        const int e = launch_train_tc(gd->net, d_samples, n, gd->wGrad, gd->gGrad, gd->dLoss, c->d_status, c->stream);
+        if (e) return cuda_fail(c, (cudaError_t)e, "guide train launch");
+        return LF_OK;
+    }
     static bool attr = false;
     if (!attr)
     {

@@ -16,6 +16,18 @@
 // The weights [out][in] are the B operands (N = out rows, K = in), so they are used as stored,
 // re-laid into core matrices once per CTA.
 //
+// Training (guide_train_tc_kernel) runs the same forward pass with every activation tile kept
+// in shared memory, then the backward pass layer by layer: the output gradient dY (one row per
+// sample, FP16) times W^T gives the previous layer's gradient (M = 128 samples, K = out), and
+// the weight gradient dW[out][in] += dY^T H sums over the tile's 128 samples as the MMA's K
+// dimension. For that product the row-per-sample tiles dY [s][out] and H [s][in] are read
+// MN-major (the transpose bits of the instruction descriptor): their 16-byte chunks run along
+// out and in, which for dW are the M and N dimensions. dY is kept 128 columns wide with zeros
+// beyond the layer's outputs, so dW is a 128-row MMA whose rows 0..63 are the layer's. The
+// four dW accumulators stay in TMEM across every tile the CTA processes and are added to the
+// global gradient once at the end; the grid-feature gradients are scattered with the
+// trilinear weights per sample, as in the warp-level kernel.
+//
 // Every wait is bounded: an mbarrier wait that runs out sets LF_DEVERR_GUIDE_TIMEOUT in the
 // status word, all threads agree on it at the next barrier, and the CTA frees its TMEM and
 // returns.
@@ -43,30 +55,34 @@ constexpr uint32_t kLbo = 128;                       // core matrices adjacent a
 constexpr uint32_t kSbo = 1024;                      // adjacent 8-row groups (8 core matrices of K = 64)
 constexpr long long kWaitCycles = 4000000000LL;      // ~2 s at 2 GHz
 
-// Byte offset of element (row, k) of a K = 64 operand in the canonical no-swizzle layout.
-__device__ __forceinline__ uint32_t cm_offset(int row, int k)
+// Byte offset of element (row, k) of an operand with kg core matrices along K (K = 8 kg) in
+// the canonical no-swizzle layout: core matrix (row / 8, k / 8) at ((row / 8) kg + k / 8) x 128.
+__device__ __forceinline__ uint32_t cm_offset(int row, int k, int kg = 8)
 {
-    return (uint32_t)(((row >> 3) * 8 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+    return (uint32_t)(((row >> 3) * kg + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Shared-memory matrix descriptor (tcgen05): start address, leading and stride byte offsets
-// (all >> 4), descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr)
+// Shared-memory matrix descriptor (tcgen05): start address, leading byte offset (between
+// core matrices adjacent along K) and stride byte offset (between core matrices adjacent along
+// M or N), all >> 4; descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo = kLbo, uint32_t sbo = kSbo)
 {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((kLbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((kSbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
     d |= (uint64_t)1 << 46;
     return d;
 }
 
 // Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B FP16 (bits 7-9, 10-12 =
-// 0), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
+// 0), A and B K-major (bits 15, 16 = 0) or MN-major (1), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N, bool aMN = false, bool bMN = false)
 {
-    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    return (1u << 4) | ((aMN ? 1u : 0u) << 15) | ((bMN ? 1u : 0u) << 16) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
@@ -119,12 +135,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void store8(unsigned char* tile, int row, int k0, const float* v)
+__device__ __forceinline__ void store8(unsigned char* tile, int row, int k0, const float* v, int kg = 8)
 {
     __half2 h[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) h[i] = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
-    *reinterpret_cast<uint4*>(tile + cm_offset(row, k0)) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(tile + cm_offset(row, k0, kg)) = *reinterpret_cast<const uint4*>(h);
+}
+
+// 8 FP16 values of a row (16 bytes) as floats.
+__device__ __forceinline__ void load8(const unsigned char* tile, int row, int k0, float* v, int kg = 8)
+{
+    const uint4 q = *reinterpret_cast<const uint4*>(tile + cm_offset(row, k0, kg));
+    const __half2* h = reinterpret_cast<const __half2*>(&q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+        v[2 * i] = __low2float(h[i]);
+        v[2 * i + 1] = __high2float(h[i]);
+    }
 }
 
 // The query's 64 input features (same values and FP16 rounding as encode_tile in lf_guide.cu)
@@ -315,6 +344,285 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         fence_after_sync();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
     }
+}
+
+namespace
+{
+// Shared memory of the training kernel, in this order so that every operand's span lies well
+// inside the allocation: dY (128 samples x 128 outputs, columns beyond the layer's outputs
+// zero), the input tile X and the activation tiles H1..H3 (128 x 64 each), the weights as
+// forward B operands [out][in] and as backward B operands W^T [in][out], then the mbarrier and
+// the TMEM address.
+constexpr int kDyBytes = 128 * 128 * 2;
+constexpr int kOffDy = 0;
+constexpr int kOffX = kOffDy + kDyBytes;
+constexpr int kOffH = kOffX + kTileBytes;                 // H1, H2, H3
+constexpr int kOffW = kOffH + 3 * kTileBytes;
+constexpr int kOffWT = kOffW + kWBytes;
+constexpr int kOffBar = kOffWT + kWBytes;
+constexpr int kTrainSmem = kOffBar + 16;
+constexpr uint32_t kTrainTmemCols = 512;                  // 2 x 64 forward/backward + 4 x 64 dW
+constexpr uint32_t kColDW = 128;                          // dW of layer l at kColDW + 64 l
+constexpr int kDyKg = 16;                                 // dY: 16 core matrices along its 128 columns
+
+// Issues one MMA group (k steps of K = 16) and commits it to the mbarrier; thread 0 only.
+__device__ __forceinline__ void issue(uint32_t dtmem, uint32_t a, uint32_t aStep, uint32_t aLbo, uint32_t aSbo, uint32_t b,
+                                      uint32_t bStep, uint32_t bLbo, uint32_t bSbo, uint32_t idesc, int steps, bool acc)
+{
+    for (int k = 0; k < steps; ++k)
+        mma_f16(dtmem, smem_desc(a + k * aStep, aLbo, aSbo), smem_desc(b + k * bStep, bLbo, bSbo), idesc,
+                (acc || k > 0) ? 1u : 0u);
+}
+}
+
+// One pass over n training samples: adds the per-sample gradients (not divided by n) of every
+// weight into gW and of every grid parameter into gGrid, and the summed loss into loss - the
+// same sums as guide_train_kernel, with the products on tcgen05.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    guide_train_tc_kernel(Net net, const float* samples, int n, float* gW, float* gGrid, float* loss,
+                          uint32_t* status)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sDy = smem + kOffDy;
+    unsigned char* sX = smem + kOffX;
+    unsigned char* sH = smem + kOffH;
+    unsigned char* sW = smem + kOffW;
+    unsigned char* sWT = smem + kOffWT;
+    uint64_t* mbarPtr = reinterpret_cast<uint64_t*>(smem + kOffBar);
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(smem + kOffBar + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t mbar = smem_addr(mbarPtr);
+
+    // weights: forward B operands [out][in] (K = in) and backward B operands [in][out]
+    // (K = out: 8 core matrices for W1..W3, 6 for W4)
+    for (int i = tid; i < kWeights; i += kTcThreads)
+    {
+        const int l = i < 3 * 4096 ? i >> 12 : 3;
+        const int o = (i - l * 4096) >> 6, k = (i - l * 4096) & 63;
+        const __half w = net.W[i];
+        *reinterpret_cast<__half*>(sW + l * kLayerBytes + cm_offset(o, k)) = w;
+        *reinterpret_cast<__half*>(sWT + l * kLayerBytes + cm_offset(k, o, l < 3 ? 8 : 6)) = w;
+    }
+    // dY columns 64..127 stay zero (the padding rows of the dW products)
+    for (int i = tid; i < kDyBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sDy)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmemSlot)),
+                     "r"(kTrainTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmemSlot;
+    const uint32_t lane0 = (uint32_t)(warp * 32) << 16;
+    const uint32_t aDy = smem_addr(sDy), aX = smem_addr(sX), aH = smem_addr(sH), aW = smem_addr(sW),
+                   aWT = smem_addr(sWT);
+    uint32_t phase = 0;
+    bool failed = false, any = false;
+    float lossSum = 0.f;
+
+    // one MMA group per call site: sync the operands written by all threads, issue, wait
+    auto run = [&](auto&& issueFn) -> bool {
+        fence_async_smem();
+        fence_before_sync();
+        __syncthreads();
+        if (tid == 0)
+        {
+            fence_after_sync();
+            issueFn();
+            mma_commit(mbar);
+        }
+        const bool ok = mbar_wait(mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok))
+        {
+            if (tid == 0) atomicOr(status, LF_DEVERR_GUIDE_TIMEOUT);
+            return false;
+        }
+        fence_after_sync();
+        return true;
+    };
+
+    const uint32_t idFwd = instr_desc(kTcRows, 64), idOut = instr_desc(kTcRows, kOut);
+    const uint32_t idDw = instr_desc(128, 64, true, true);
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    for (int tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x)
+    {
+        const int q = tile * kTcRows + tid;
+        const bool valid = q < n;
+        const float* rec = samples + (size_t)(valid ? q : 0) * kSampleFloats;
+        encode_row(net, rec, valid, sX, tid);
+        // forward: H1..H3 = relu(A W^T) into their tiles, outputs into registers
+        float out[48];
+        for (int layer = 0; layer < 4 && !failed; ++layer)
+        {
+            const uint32_t a = layer == 0 ? aX : aH + (layer - 1) * kTileBytes;
+            const uint32_t dcol = (uint32_t)(layer & 1) * 64u;
+            failed = !run([&] { issue(tmem + dcol, a, 256, kLbo, kSbo, aW + layer * kLayerBytes, 256, kLbo, kSbo,
+                                      layer < 3 ? idFwd : idOut, 4, false); });
+            if (failed) break;
+            if (layer < 3)
+            {
+                unsigned char* h = sH + layer * kTileBytes;
+#pragma unroll
+                for (int c = 0; c < 64; c += 16)
+                {
+                    float v[16];
+                    tmem_ld16(tmem + lane0 + dcol + c, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+                    store8(h, tid, c, v);
+                    store8(h, tid, c + 8, v + 8);
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int c = 0; c < kOut; c += 16) tmem_ld16(tmem + lane0 + dcol + c, out + c);
+                tmem_wait_ld();
+            }
+        }
+        if (failed) break;
+        // loss and the output gradient (40 used of 48; columns 40..63 zero)
+        {
+            float d[64];
+#pragma unroll
+            for (int k = 0; k < 64; ++k) d[k] = 0.f;
+            if (valid) lossSum += sample_loss_grad(out, rec + 9, rec[12], d);
+#pragma unroll
+            for (int k0 = 0; k0 < 64; k0 += 8) store8(sDy, tid, k0, d + k0, kDyKg);
+        }
+        // backward, layer 4 .. 1: dH = dY W (into the free forward column half) and
+        // dW += dY^T H (accumulated across tiles); then dY of the layer below = dH * relu'(H)
+        for (int layer = 3; layer >= 0 && !failed; --layer)
+        {
+            const uint32_t dcol = (uint32_t)(layer & 1) * 64u;
+            const uint32_t hIn = layer == 0 ? aX : aH + (layer - 1) * kTileBytes;   // this layer's input
+            const int kSteps = layer == 3 ? 3 : 4;                                   // K = 48 or 64 outputs
+            const int nIn = layer == 0 ? 32 : 64;                                    // input gradients needed
+            const bool accW = any;
+            failed = !run([&] {
+                // dH[s][in] = sum_out dY[s][out] W[out][in]: A = dY (K-major, K = out), B = W^T
+                issue(tmem + dcol, aDy, 256, kLbo, kDyKg * 128, aWT + layer * kLayerBytes, 256, kLbo,
+                      (layer < 3 ? 8 : 6) * 128, instr_desc(kTcRows, nIn), kSteps, false);
+                // dW[out][in] += sum_s dY[s][out] H[s][in]: A = dY^T (MN-major, M = 128 padded
+                // outputs), B = H^T (MN-major, N = 64 inputs); K = the tile's 128 samples
+                issue(tmem + kColDW + 64 * layer, aDy, 2 * kDyKg * 128, kDyKg * 128, 128, hIn, 2 * 1024, 1024, 128,
+                      idDw, 8, accW);
+            });
+            if (failed) break;
+            if (layer > 0)
+            {
+                // dY of layer - 1 = dH masked by the ReLU of H_layer (its FP16 activations > 0)
+                const unsigned char* h = sH + (layer - 1) * kTileBytes;
+#pragma unroll
+                for (int c = 0; c < 64; c += 16)
+                {
+                    float v[16], hv[16];
+                    tmem_ld16(tmem + lane0 + dcol + c, v);
+                    tmem_wait_ld();
+                    load8(h, tid, c, hv);
+                    load8(h, tid, c + 8, hv + 8);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = hv[i] > 0.f ? v[i] : 0.f;
+                    store8(sDy, tid, c, v, kDyKg);
+                    store8(sDy, tid, c + 8, v + 8, kDyKg);
+                }
+            }
+            else
+            {
+                // grid-feature gradients (inputs 0..31) scattered with the trilinear weights; the
+                // warp-wide TMEM loads run on every lane, the scatter on valid samples only
+                float dx[32];
+#pragma unroll
+                for (int c = 0; c < 32; c += 16) tmem_ld16(tmem + lane0 + dcol + c, dx + c);
+                tmem_wait_ld();
+                float p01[3];
+                position01(net, rec, p01);
+#pragma unroll 1
+                for (int l = 0; l < (valid ? kLevels : 0); ++l)
+                {
+                    uint32_t idx[8];
+                    float w[8];
+                    grid_corners(net.res[l], p01, idx, w);
+                    float* gt = gGrid + (size_t)l * kT * kFeatures;
+                    float g4[4];
+#pragma unroll
+                    for (int f = 0; f < 4; ++f)
+                    {
+                        g4[f] = dx[0];
+#pragma unroll
+                        for (int qq = 0; qq < 32; ++qq)
+                            if (qq == l * 4 + f) g4[f] = dx[qq];
+                    }
+                    for (int c = 0; c < 8; ++c)
+                        for (int f = 0; f < 4; ++f) atomicAdd(&gt[(size_t)idx[c] * kFeatures + f], w[c] * g4[f]);
+                }
+            }
+        }
+        any = true;
+    }
+    // loss: block sum, one atomic
+    for (int off = 16; off > 0; off >>= 1) lossSum += __shfl_xor_sync(0xffffffffu, lossSum, off);
+    if ((tid & 31) == 0 && lossSum != 0.f) atomicAdd(loss, lossSum);
+    // weight gradients: TMEM lanes 0..63 = outputs, 64 columns = inputs, one atomic each
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (!failed && any && warp < 2)
+    {
+        for (int layer = 0; layer < 4; ++layer)
+        {
+            const int o = tid;   // lanes 0..63: warps 0 and 1
+            const int outs = layer < 3 ? 64 : kOut;
+            const int base = layer * 4096;
+            for (int c = 0; c < 64; c += 16)
+            {
+                float v[16];
+                tmem_ld16(tmem + lane0 + kColDW + 64 * layer + c, v);
+                tmem_wait_ld();
+                if (o < outs)
+                    for (int i = 0; i < 16; ++i)
+                        if (v[i] != 0.f) atomicAdd(&gW[base + o * 64 + c + i], v[i]);
+            }
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0)
+    {
+        fence_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrainTmemCols)
+                     : "memory");
+    }
+}
+
+int launch_train_tc(const Net& net, const float* samples, int n, float* gW, float* gGrid, float* loss, uint32_t* status,
+                    cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(guide_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
+        attr = true;
+    }
+    int sms = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // one CTA per SM: its 512 TMEM columns are the SM's
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int blocks = std::max(1, std::min(sms, tiles));
+    guide_train_tc_kernel<<<blocks, kTcThreads, kTrainSmem, st>>>(net, samples, n, gW, gGrid, loss, status);
+    return (int)cudaGetLastError();
 }
 
 int launch_infer_tc(const Net& net, const float* queries, const int* nDev, int cap, float* mix, uint32_t* status,

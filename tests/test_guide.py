@@ -66,7 +66,10 @@ def flat_params(grid, W):
 
 
 @pytest.mark.gpu
-def test_device_gradients_match_fp64_oracle(ctx):
+@pytest.mark.parametrize("tensor", [False, True])
+def test_device_gradients_match_fp64_oracle(ctx, tensor):
+    """Loss, weight and grid gradients of the warp-level mma.sync kernel and of the tcgen05
+    kernel (128-sample tiles; 1000 samples end on a partial tile) against the FP64 oracle."""
     grid, W = G.init_params(7)
     grid = [g * 2e3 for g in grid]             # grid features of order 0.1
     wflat, gflat = flat_params(grid, W)
@@ -77,7 +80,9 @@ def test_device_gradients_match_fp64_oracle(ctx):
     gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1])
     try:
         gd.set_params(wflat, gflat)
+        gd.set_tensor_path(tensor)
         loss, dw, dg = gd.gradients(records(p, wo, nrm, wd, w))
+        assert ctx.device_errors() == 0
     finally:
         gd.close()
     ref_loss, ref_dW, ref_dg, _ = G.loss_and_grads(grid16, W16, p, wo, nrm, wd, w)
@@ -114,11 +119,13 @@ def test_device_pdf_matches_oracle(ctx):
 
 
 @pytest.mark.gpu
-def test_training_fits_a_position_dependent_distribution(ctx):
+@pytest.mark.parametrize("tensor", [False, True])
+def test_training_fits_a_position_dependent_distribution(ctx, tensor):
     """Directions concentrated around an axis that depends on position: Adam on the GPU lowers
     the loss well below that of the initial (nearly uniform) mixture."""
     rng = np.random.default_rng(6)
     gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1], seed=1)
+    gd.set_tensor_path(tensor)
 
     def batch(n):
         p = rng.uniform(0, 1, (n, 3))
