@@ -407,27 +407,40 @@ def run_serving(ctx, n_jobs, max_spp=256, budget_gb=0.0, rate=20.0, low_load=0.5
         p.width, p.height, p.max_depth = j["width"], j["height"], j["depth"]
         return p
 
-    def one_run(arrival_rate):
+    def one_run(arrival_rate, limit_s=600.0):
         srv = lf.Server(ctx, memory_budget=budget)
         sids = [srv.add_scene(sc) for _, sc in pool]
-        t0 = time.perf_counter()
-        ids = []
-        due = 0.0
-        for j in jobs:
-            if arrival_rate:
-                due += j["gap"] / arrival_rate
-                wait = due - (time.perf_counter() - t0)
-                if wait > 0:
-                    time.sleep(wait)
-            ids.append(srv.submit(sids[j["scene"]], params(j), j["spp"]))
-        for jid in ids:
-            srv.wait(jid)
-        wall = time.perf_counter() - t0
-        infos = [srv.info(jid) for jid in ids]
-        st = srv.stats()
-        for jid in ids:
-            srv.release(jid)
-        srv.close()
+        pending, infos = [], {}
+
+        def reap():
+            # a client reads and releases each job as it finishes, so finished jobs do not
+            # hold budget that later jobs need
+            for jid in list(pending):
+                if srv.wait(jid, 0):
+                    infos[jid] = srv.info(jid)
+                    srv.release(jid)
+                    pending.remove(jid)
+
+        try:
+            t0 = time.perf_counter()
+            due = 0.0
+            for j in jobs:
+                if arrival_rate:
+                    due += j["gap"] / arrival_rate
+                    while due - (time.perf_counter() - t0) > 0:
+                        reap()
+                        time.sleep(min(0.002, max(0.0, due - (time.perf_counter() - t0))))
+                pending.append(srv.submit(sids[j["scene"]], params(j), j["spp"]))
+            while pending:
+                reap()
+                if time.perf_counter() - t0 > limit_s:
+                    raise RuntimeError(f"serving run exceeded {limit_s} s with {len(pending)} jobs left")
+                time.sleep(0.001)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        finally:
+            srv.close()
+        infos = list(infos.values())
         lat = np.array([i["finish_ms"] - i["submit_ms"] for i in infos])
         span = (max(i["finish_ms"] for i in infos) - min(i["submit_ms"] for i in infos)) / 1e3
         return {"arrival_rate_per_s": arrival_rate or None, "wall_s": wall, "makespan_s": span,

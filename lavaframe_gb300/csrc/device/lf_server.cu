@@ -34,6 +34,7 @@ struct ServerScene
     size_t bytes = 0;          // device bytes when resident (estimate before the first upload)
     uint64_t lastUse = 0;
     int users = 0;             // queued + running jobs
+    int running = 0;           // running jobs: the scene may be evicted only when none runs
 };
 
 struct ServerPass
@@ -131,8 +132,10 @@ size_t job_need(const lf_server* s, const ServerJob& j)
     return pix * sizeof(float4) + (size_t)passes * std::min<size_t>(perPass, (size_t)j.spp) * pix * sizeof(float4);
 }
 
-// Evicts idle resident scenes (least recently used first) until `need` more bytes fit.
-bool make_room(lf_server* s, size_t need)
+// Evicts idle resident scenes (no running job; least recently used first) until `need` more
+// bytes fit. A scene that only queued jobs refer to is idle: it is uploaded again when one of
+// them is admitted.
+bool make_room(lf_server* s, size_t need, const ServerScene* keep)
 {
     const uint64_t budget = s->cfg.memory_budget;
     while (s->deviceBytes + need > budget)
@@ -141,7 +144,7 @@ bool make_room(lf_server* s, size_t need)
         for (auto& kv : s->scenes)
         {
             ServerScene& sc = kv.second;
-            if (sc.dev && sc.users == 0 && (!victim || sc.lastUse < victim->lastUse)) victim = &sc;
+            if (&sc != keep && sc.dev && sc.running == 0 && (!victim || sc.lastUse < victim->lastUse)) victim = &sc;
         }
         if (!victim) return false;
         lf_scene_release(victim->dev);
@@ -158,7 +161,7 @@ bool admit(lf_server* s, ServerJob& j)
     lf_ctx* c = s->ctx;
     ServerScene& sc = s->scenes[j.scene];
     const size_t need = job_need(s, j) + (sc.dev ? 0 : sc.bytes);
-    if (!make_room(s, need)) return false;
+    if (!make_room(s, need, &sc)) return false;
     if (!sc.dev)
     {
         lf_scene* dev = nullptr;
@@ -183,6 +186,7 @@ bool admit(lf_server* s, ServerJob& j)
     cudaMemsetAsync(j.accum, 0, j.accumBytes, c->stream);
     j.passReserve = job_need(s, j) - j.accumBytes;
     s->deviceBytes += j.accumBytes + j.passReserve;
+    sc.running++;
     j.state = LF_JOB_RUNNING;
     j.startMs = now_ms(s);
     return true;
@@ -238,8 +242,25 @@ void scheduler(lf_server* s)
             ServerJob& j = s->jobs[s->queue.front()];
             std::lock_guard<std::recursive_mutex> g(c->mu);
             cudaSetDevice(c->device);
-            if (!admit(s, j)) break;
+            if (admit(s, j))
+            {
+                s->queue.pop_front();
+                continue;
+            }
+            bool anyRunning = false;
+            for (auto& kv : s->jobs)
+                if (kv.second.state == LF_JOB_RUNNING) anyRunning = true;
+            if (anyRunning) break;   // running jobs will free their reservations
+            // Nothing runs and every idle scene is evicted, yet the job does not fit: the
+            // budget is held by finished jobs whose buffers were not released. Fail the job
+            // instead of waiting for memory that nothing will free.
+            s->err = "job " + std::to_string(j.id) +
+                     " cannot be admitted: the memory budget is held by finished jobs that were not released";
+            j.state = LF_JOB_FAILED;
+            j.finishMs = now_ms(s);
+            s->scenes[j.scene].users--;
             s->queue.pop_front();
+            s->doneCv.notify_all();
         }
         // 2. passes
         bool published = false;
@@ -275,6 +296,7 @@ void scheduler(lf_server* s)
                 j.passReserve = 0;
                 s->stats.jobs_done++;
                 s->scenes[j.scene].users--;
+                s->scenes[j.scene].running--;
                 s->scenes[j.scene].lastUse = ++s->useClock;
                 engine_job_free(e, j.engineJob);
                 j.engineJob = -1;

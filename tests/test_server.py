@@ -147,3 +147,37 @@ def test_wait_times_out_then_completes(ctx):
         assert srv.info(jid)["samples_done"] == 64
     finally:
         srv.close()
+
+
+def test_unreleased_jobs_fail_the_next_job_instead_of_blocking(ctx):
+    """A budget that holds one job: while a finished job's buffers are not released, a job that
+    does not fit fails at once (nothing running would free memory) instead of waiting forever;
+    after the release the next job runs."""
+    s = lf.HostScene().gen_icospheres(4, 4, 7, 64, 32).build()
+    pool = ctx_pool_bytes(ctx)
+    ds = ctx.upload(s)
+    scene_bytes = ds.device_bytes()
+    ds.close()
+    p = s.render_params()
+    p.width, p.height = 32, 18
+    pix = p.width * p.height
+    need = pix * 16 + 2 * pix * 16              # accumulation + one pass of 2 samples
+    srv = lf.Server(ctx, memory_budget=pool + scene_bytes + need + 1024, paths_per_pass=4096, passes_per_job=1)
+    try:
+        sid = srv.add_scene(s)
+        j1 = srv.submit(sid, p, 2)
+        assert srv.wait(j1, 60000)
+        j2 = srv.submit(sid, p, 2)
+        with pytest.raises(lf.LFError):
+            srv.wait(j2, 60000)
+        assert srv.info(j2)["state"] == lf.JOB_FAILED
+        assert "not released" in ctx.error()
+        img1 = srv.read(j1)
+        srv.release(j1)
+        srv.release(j2)
+        j3 = srv.submit(sid, p, 2)
+        assert srv.wait(j3, 60000)
+        assert srv.read(j3).tobytes() == img1.tobytes()
+        srv.release(j3)
+    finally:
+        srv.close()
