@@ -637,10 +637,10 @@ int launch_infer_tc(const Net& net, const float* queries, const int* nDev, int c
     int sms = 1, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // at most 4 CTAs per SM: 4 x 128 TMEM columns fill the SM's 512, so no allocation waits
-    const int perSm = std::min(4, occupancy_blocks_per_sm((const void*)guide_infer_tc_kernel, kTcThreads, kTcSmem));
+    // 3 CTAs per SM: the registers (162 per thread) fit 3, shared memory (47 KB) 4, and 3 x 128
+    // TMEM columns stay within the SM's 512, so no allocation waits
     const int tiles = (cap + kTcRows - 1) / kTcRows;
-    const int blocks = std::max(1, std::min(sms * std::max(1, perSm), tiles));
+    const int blocks = std::max(1, std::min(sms * 3, tiles));
     guide_infer_tc_kernel<<<blocks, kTcThreads, kTcSmem, st>>>(net, queries, cap, nDev, mix, status);
     return (int)cudaGetLastError();
 }
