@@ -99,13 +99,26 @@ __device__ __forceinline__ void position01(const Net& net, const float p[3], flo
     for (int a = 0; a < 3; ++a) p01[a] = (p[a] - net.lo[a]) * net.invExt[a];
 }
 
-// von Mises-Fisher lobe parameters from raw outputs (same mapping as the oracle).
+// von Mises-Fisher lobe of the sampling mixture from raw outputs (the oracle's `pdf`): the mean
+// direction is normalised exactly (a raw vector of zero length gives +z), so that mix_sample
+// draws unit directions whose density is exactly mix_pdf. The training loss keeps the
+// regularised mean mu_raw / sqrt(|mu_raw|^2 + 1e-6) (sample_loss_grad); the two differ only for
+// near-zero raw vectors, whose lobes would otherwise sample directions of less than unit length.
 __device__ __forceinline__ void lobe_params(const float* o5, float mu[3], float* kappa)
 {
-    const float nrm = sqrtf(o5[0] * o5[0] + o5[1] * o5[1] + o5[2] * o5[2] + 1e-6f);
-    mu[0] = o5[0] / nrm;
-    mu[1] = o5[1] / nrm;
-    mu[2] = o5[2] / nrm;
+    const float len = sqrtf(o5[0] * o5[0] + o5[1] * o5[1] + o5[2] * o5[2]);
+    if (len > 1e-30f)
+    {
+        mu[0] = o5[0] / len;
+        mu[1] = o5[1] / len;
+        mu[2] = o5[2] / len;
+    }
+    else
+    {
+        mu[0] = 0.f;
+        mu[1] = 0.f;
+        mu[2] = 1.f;
+    }
     *kappa = __expf(fminf(fmaxf(o5[3], -3.f), 7.f));
 }
 

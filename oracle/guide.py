@@ -11,7 +11,9 @@ The model (identical definition to the device kernels in lavaframe_gb300/csrc/de
   mixture     = 8 von Mises-Fisher lobes from outputs 0..39, per lobe (mu_raw xyz, kappa_raw,
                 logit): mu = mu_raw / sqrt(|mu_raw|^2 + 1e-6), kappa = exp(clamp(kappa_raw, -3, 7)),
                 weights = softmax(logits); pdf(w) = sum_i pi_i k_i / (2 pi (1 - exp(-2 k_i)))
-                * exp(k_i (mu_i . w - 1));
+                * exp(k_i (mu_i . w - 1)); the sampling mixture (`pdf`, what guided rendering
+                draws from) normalises mu_i exactly, mu_raw / |mu_raw|, so that it is a density of
+                unit directions; the loss keeps the regularised mean above;
   loss        = mean over samples of -weight * log(pdf(direction) + 1e-12): weighted maximum
                 likelihood of directions sampled by the tracer, weighted by the luminance of the
                 incident radiance they carried over the pdf they were sampled with (the KL
@@ -128,8 +130,11 @@ def vmf(mu, kap, w):
 
 
 def pdf(out, w):
-    mu, kap, pi, *_ = mixture(out)
-    f, _ = vmf(mu, kap, w)
+    """Density of the sampling mixture: lobe means normalised exactly (zero raw vectors: +z)."""
+    _, kap, pi, raw, *_ = mixture(out)
+    ln = np.sqrt((raw * raw).sum(-1))
+    unit = np.where(ln[..., None] > 1e-30, raw / np.maximum(ln, 1e-300)[..., None], np.array([0.0, 0.0, 1.0]))
+    f, _ = vmf(unit, kap, w)
     return (pi * f).sum(1)
 
 

@@ -182,3 +182,32 @@ def test_tcgen05_inference_matches_warp_mma_and_oracle(ctx, n):
     assert rel.max() < 0.15, rel.max()
     rel_w = np.abs(pdf_w[:m] - ref) / (np.abs(ref) + 1e-4)
     assert np.median(rel) < 2 * np.median(rel_w) + 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tensor", [False, True])
+def test_sampling_mixture_means_are_unit_vectors(ctx, tensor):
+    """Lobes whose raw mean vectors are near zero (an untrained or collapsing lobe) still sample
+    unit directions: the mixture the guided shade draws from normalises every mean exactly, and
+    its pdf is the oracle's sampling density."""
+    grid, W = G.init_params(13)
+    grid = [g * 2e3 for g in grid]
+    W = [x.copy() for x in W]
+    for i in range(8):
+        W[3][5 * i:5 * i + 3] *= 1e-4          # mean rows of every lobe: |mu_raw| ~ 1e-5
+    wflat, gflat = flat_params(grid, W)
+    p, wo, nrm, wd, w = random_batch(700, 7)
+    gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1])
+    try:
+        gd.set_params(wflat, gflat)
+        gd.set_tensor_path(tensor)
+        mix, pdf = gd.eval(records(p, wo, nrm, wd, w))
+    finally:
+        gd.close()
+    mu = mix.reshape(-1, 8, 5)[:, :, 0:3]
+    np.testing.assert_allclose(np.linalg.norm(mu, axis=-1), 1.0, atol=1e-5)
+    x, _ = G.encode([G.f16(g) for g in grid], p, wo, nrm)
+    _, out = G.forward([G.f16(v) for v in W], G.f16(x))
+    ref = G.pdf(out, wd)
+    rel = np.abs(pdf - ref) / (np.abs(ref) + 1e-4)
+    assert (rel < 3e-2).mean() > 0.99, (rel < 3e-2).mean()
