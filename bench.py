@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768/1024; 0 = 512)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
     ap.add_argument("--sort-by-material", action="store_true", help="render workloads: engine sort-by-material")
+    ap.add_argument("--engine-drain", type=int, default=-1, help="render workloads: engine drain threshold (paths)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
@@ -549,6 +550,8 @@ def main():
     ctx = lf.Context(local)
     if args.engine_slots or args.shade_cap:
         ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 512)
+    if args.engine_drain >= 0:
+        ctx.set_engine_drain(args.engine_drain)
     if args.workload == "c4":
         cw, ch = (int(x) for x in args.c4_size.split("x"))
         r = run_guiding(ctx, cw, ch, args.c4_ref_spp, batch=args.c4_batch, every=args.c4_every, alpha=args.c4_alpha,

@@ -301,6 +301,11 @@ lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend
  * unchanged either way. The buckets take 16 B per path slot, allocated on first use. Fails
  * with LF_ERR_STATE while passes are in flight. */
 lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material);
+/* Engine drain threshold (no counterpart in the reference): once every path id of a frame run
+ * is issued and at most `paths` paths are still in flight, the run finishes them with one
+ * kernel that takes each path through its remaining bounces instead of a further step pair per
+ * bounce (default 2^22; 0 = never). Results are unchanged. */
+lf_status lf_ctx_set_engine_drain(lf_ctx* c, int64_t paths);
 /* Current pool size and device bytes of the engine (0, 0 before first use). */
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 

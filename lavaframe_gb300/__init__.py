@@ -68,6 +68,7 @@ _SIG = {
     "lf_ctx_configure_engine": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "lf_ctx_set_host_chunks": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_set_engine_sort": (C.c_int, [_P, C.c_int32]),
+    "lf_ctx_set_engine_drain": (C.c_int, [_P, C.c_int64]),
     "lf_ctx_kernel_timer": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_device_attrs": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lf_ctx_kernel_timer_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
@@ -399,6 +400,10 @@ class Context:
         ms, n = C.c_double(), C.c_int64()
         self._c(lib().lf_ctx_kernel_timer_read(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def set_engine_drain(self, paths):
+        """Paths in flight at which a frame run switches to the one-kernel drain (0 = never)."""
+        self._c(lib().lf_ctx_set_engine_drain(self.h, int(paths)))
 
     def set_engine_sort(self, sort_by_material):
         """Engine sort-by-material: shade takes the paths that hit a surface grouped by the class

@@ -1,8 +1,9 @@
 """Autotuner of the path engine (no reference counterpart).
 
 Chooses the engine's pool size (paths in flight), the block sizes of its extend and shadow
-kernels, the register cap of its shade kernel and whether shade takes the surface hits sorted
-by material class, by timing short renders of the workload itself on the GPU, one knob at a
+kernels, the register cap of its shade kernel, whether shade takes the surface hits sorted
+by material class, and the number of paths in flight at which a run switches to its one-kernel
+drain, by timing short renders of the workload itself on the GPU, one knob at a
 time (coordinate descent from the current setting). The
 result is applied to the context and can be cached in a JSON file keyed by the workload
 signature (resolution, samples, depth, triangles).
@@ -18,9 +19,10 @@ CANDIDATES = {
     "block_extend": [64, 128, 256],
     "block_shadow": [64, 128, 256],
     "sort_by_material": [0, 1],
+    "drain_paths": [1 << 21, 1 << 22, 1 << 23],
 }
 DEFAULT = {"slots": 1 << 24, "shade_threads_per_sm": 512, "block_extend": 128, "block_shadow": 128,
-           "sort_by_material": 0}
+           "sort_by_material": 0, "drain_paths": 1 << 22}
 MARGIN = 0.02   # a setting replaces the current one only when it is this much faster (timing noise)
 
 
@@ -32,6 +34,7 @@ def _apply(ctx, cfg):
     ctx.configure_engine(slots=cfg["slots"], block_extend=cfg["block_extend"], block_shade=128,
                          block_shadow=cfg["block_shadow"], shade_threads_per_sm=cfg["shade_threads_per_sm"])
     ctx.set_engine_sort(cfg.get("sort_by_material", 0))
+    ctx.set_engine_drain(cfg.get("drain_paths", 1 << 22))
 
 
 def apply_default(ctx):
