@@ -61,7 +61,6 @@ def parse():
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
     ap.add_argument("--sort-by-material", action="store_true", help="render workloads: engine sort-by-material")
     ap.add_argument("--engine-drain", type=int, default=-1, help="render workloads: engine drain threshold (paths)")
-    ap.add_argument("--engine-refill", type=int, default=-1, help="render workloads: extend with per-lane refill (1)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
     ap.add_argument("--c4-size", default="1280x720", help="guiding workload resolution WxH")
@@ -563,8 +562,6 @@ def main():
         ctx.configure_engine(slots=args.engine_slots, shade_threads_per_sm=args.shade_cap or 512)
     if args.engine_drain >= 0:
         ctx.set_engine_drain(args.engine_drain)
-    if args.engine_refill >= 0:
-        ctx.set_engine_refill(args.engine_refill)
     if args.workload == "c4":
         cw, ch = (int(x) for x in args.c4_size.split("x"))
         paths = (0, 1) if args.c4_tensor < 0 else (args.c4_tensor,)

@@ -306,11 +306,6 @@ lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material);
  * kernel that takes each path through its remaining bounces instead of a further step pair per
  * bounce (default 2^22; 0 = never). Results are unchanged. */
 lf_status lf_ctx_set_engine_drain(lf_ctx* c, int64_t paths);
-/* Engine extension with per-lane refill (no counterpart in the reference): in single-job steps
- * each lane of an extend warp takes a new path as soon as its ray is traced, once 8 lanes are
- * idle, instead of the warp taking 32 paths at a time and waiting for the longest (1 = on,
- * 0 = off, default). Hits are identical. Fails with LF_ERR_STATE while passes are in flight. */
-lf_status lf_ctx_set_engine_refill(lf_ctx* c, int32_t refill);
 /* Current pool size and device bytes of the engine (0, 0 before first use). */
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes);
 

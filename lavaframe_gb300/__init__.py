@@ -69,7 +69,6 @@ _SIG = {
     "lf_ctx_set_host_chunks": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_set_engine_sort": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_set_engine_drain": (C.c_int, [_P, C.c_int64]),
-    "lf_ctx_set_engine_refill": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_kernel_timer": (C.c_int, [_P, C.c_int32]),
     "lf_ctx_device_attrs": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lf_ctx_kernel_timer_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
@@ -401,10 +400,6 @@ class Context:
         ms, n = C.c_double(), C.c_int64()
         self._c(lib().lf_ctx_kernel_timer_read(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
-
-    def set_engine_refill(self, refill):
-        """Engine extend with per-lane refill (identical hits)."""
-        self._c(lib().lf_ctx_set_engine_refill(self.h, 1 if refill else 0))
 
     def set_engine_drain(self, paths):
         """Paths in flight at which a frame run switches to the one-kernel drain (0 = never)."""

@@ -321,106 +321,6 @@ __global__ void __maxnreg__(72) engine_extend_kernel(EngineBuffers b, EngineJob 
     }
 }
 
-// Extend with per-lane refill (single-job steps): every lane keeps its own traversal state
-// and, once at least kRefillLanes lanes of the warp have finished their rays, the idle lanes
-// take the next queue entries together (one atomic per warp), so a warp does not wait for its
-// longest ray before starting new ones. Each ray's traversal is the same step sequence as in
-// engine_extend_kernel, so hits are identical; only the order of the hit/miss lists differs.
-constexpr int kRefillLanes = 8;
-constexpr int kRefillSteps = 16;   // traversal steps between refill checks
-
-// The whole closest-hit query of a ray the wide traversal does not take (degenerate direction
-// or binary traversal selected); out of line, so its state stays out of the refill loop.
-__device__ __noinline__ Hit closest_hit_out_of_line(const DevScene S, v3 o, v3 d, bool lights, uint32_t* status)
-{
-    Hit h;
-    set_error(status, closest_hit<false>(S, o, d, kInfinity, lights, &h, nullptr));
-    return h;
-}
-
-__global__ void __maxnreg__(72) engine_extend_refill_kernel(EngineBuffers b, EngineJob one, int parity)
-{
-    const int n = b.ctl->count[parity];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr[1], (unsigned long long)n);
-    const int* q = b.queue[parity];
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    const DevScene& S = one.S.trav;
-    const bool lights = one.P.useLights != 0;
-    int stack[kWideStack];
-    WideRay w;
-    Hit h;
-    int p = -1;
-    bool active = false, exhausted = false;
-    while (true)
-    {
-        bool finished = false;
-        const unsigned idle = __ballot_sync(kFull, !active);
-        if (!exhausted && __popc(idle) >= kRefillLanes)
-        {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&b.ctl->extendNext, __popc(idle));
-            base = __shfl_sync(kFull, base, 0);
-            if (base + __popc(idle) >= n) exhausted = true;
-            const int i = base + __popc(idle & below);
-            if (!active && i < n)
-            {
-                p = q[i];
-                const float4 o4 = b.ps.o[p], d4 = b.ps.d[p];
-                const v3 o = f3(o4), d = f3(d4);
-                h.inst = -1;
-                h.prim = -1;
-                h.light = -1;
-                float t0 = kInfinity;
-                if (lights) t0 = lights_closest(S, o, d, kInfinity, &h.light);
-                bool fast;
-                const v3 winvd = inv_dir(d, &fast);
-                if (S.wnodes && S.wideOn && fast)
-                {
-                    wide_init(S, w, o, d, winvd, t0);
-                    active = true;
-                }
-                else
-                {
-                    // degenerate direction (or binary traversal selected): the whole query now
-                    h = closest_hit_out_of_line(S, o, d, lights, b.status);
-                    finished = true;
-                }
-            }
-        }
-        if (exhausted && !__any_sync(kFull, active || finished)) break;
-        if (active)
-        {
-            for (int k = 0; k < kRefillSteps; ++k)
-                if (wide_step<false>(S, w, stack, h))
-                {
-                    h.t = w.t;
-                    set_error(b.status, w.err);
-                    active = false;
-                    finished = true;
-                    break;
-                }
-        }
-        bool miss = false;
-        if (finished)
-        {
-            b.ps.hit[p] = make_float4(h.t, __int_as_float(h.inst), __int_as_float(h.prim), __int_as_float(h.light));
-            miss = h.t == kInfinity;
-        }
-        const unsigned hm = __ballot_sync(kFull, finished && !miss), mm = __ballot_sync(kFull, finished && miss);
-        int hb = 0, mb = 0;
-        if (lane == 0)
-        {
-            if (hm) hb = atomicAdd(&b.ctl->hitCount, __popc(hm));
-            if (mm) mb = atomicAdd(&b.ctl->missCount, __popc(mm));
-        }
-        hb = __shfl_sync(kFull, hb, 0);
-        mb = __shfl_sync(kFull, mb, 0);
-        if (finished && !miss) b.part[hb + __popc(hm & below)] = p;
-        if (finished && miss) b.part[b.cap - 1 - (mb + __popc(mm & below))] = p;
-    }
-}
-
 // Blocks of at most 256 threads. kThreadsPerSm > 0 caps registers so that many threads fit on
 // an SM (512: 128 registers, no spills; 768: 85 registers, a few spills; 1024: 64 registers);
 // 0 leaves the compiler's choice.
@@ -653,12 +553,8 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
     const int be = b.blockExtend > 0 ? b.blockExtend : 128;
     const int bs = b.blockShade > 0 ? b.blockShade : 128;
     const int bw = b.blockShadow > 0 ? b.blockShadow : 128;
-    if (kOne && b.extendRefill && !b.sortByMaterial)
-        engine_extend_refill_kernel<<<full_grid((const void*)engine_extend_refill_kernel, be, b.cap), be, 0, st>>>(
-            b, one, parity);
-    else
-        engine_extend_kernel<kOne><<<full_grid((const void*)engine_extend_kernel<kOne>, be, b.cap), be, 0, st>>>(
-            b, one, parity);
+    engine_extend_kernel<kOne><<<full_grid((const void*)engine_extend_kernel<kOne>, be, b.cap), be, 0, st>>>(b, one,
+                                                                                                           parity);
     if (b.shadeThreadsPerSm == 512 && kOne && !one.P.useLights)
         engine_shade_kernel<kOne, 512, false><<<full_grid((const void*)engine_shade_kernel<kOne, 512, false>, bs, b.cap),
                                                 bs, 0, st>>>(b, one, parity);

@@ -70,7 +70,6 @@ struct EngineBuffers
     int* part;                   // extended paths: hits from the front, misses from the back
     int* partSort;               // sort-by-material: hits of class k at [k * cap, k * cap + bucketCount[k])
     int sortByMaterial;          // 1: extend buckets hits by material class, shade takes them class by class
-    int extendRefill;            // 1: extend lanes fetch a new path as soon as theirs ends (single-job steps)
     ShadowRec* shadow;
     int* done[2];                // slots whose path finished
     EngineCtl* ctl;

@@ -189,16 +189,6 @@ lf_status engine_set_sort(EngineHost* e, bool on)
     return LF_OK;
 }
 
-lf_status engine_set_refill(EngineHost* e, bool on)
-{
-    lf_ctx* c = e->c;
-    if (e->active > 0) return fail(c, LF_ERR_STATE, "engine has passes in flight");
-    cudaStreamSynchronize(c->stream);
-    e->b.extendRefill = on ? 1 : 0;
-    drop_graphs(e);   // the graphs hold the kernel parameters
-    return LF_OK;
-}
-
 int engine_job_alloc(EngineHost* e, const ShadeScene& S, const Params& P)
 {
     for (int j = 0; j < kMaxJobs; ++j)

@@ -45,8 +45,6 @@ lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockS
 // Sort-by-material on or off: extend buckets the hits by material class (4 x slots queue
 // entries, allocated on first use) and shade takes them class by class.
 lf_status engine_set_sort(EngineHost* e, bool on);
-// Extend with per-lane refill on or off (single-job steps without sort-by-material).
-lf_status engine_set_refill(EngineHost* e, bool on);
 int engine_job_alloc(EngineHost* e, const ShadeScene& S, const Params& P);
 void engine_job_write(EngineHost* e, int job, const ShadeScene& S, const Params& P);
 void engine_job_free(EngineHost* e, int job);

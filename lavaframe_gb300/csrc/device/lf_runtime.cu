@@ -1704,17 +1704,6 @@ lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend
     return engine_configure(e, slots, block_extend, block_shade, block_shadow, shade_threads_per_sm);
 }
 
-lf_status lf_ctx_set_engine_refill(lf_ctx* c, int32_t refill)
-{
-    if (!c || refill < 0 || refill > 1) return LF_ERR_INVALID;
-    std::lock_guard<std::recursive_mutex> lk(c->mu);
-    cudaSetDevice(c->device);
-    EngineHost* e = nullptr;
-    lf_status st = engine_get(c, &e);
-    if (st != LF_OK) return st;
-    return engine_set_refill(e, refill != 0);
-}
-
 lf_status lf_ctx_set_engine_drain(lf_ctx* c, int64_t paths)
 {
     if (!c || paths < 0) return LF_ERR_INVALID;

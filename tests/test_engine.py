@@ -105,29 +105,6 @@ def test_sort_by_material_keeps_results(ctx, slots):
     assert same_bits(got["accum"], ref_acc)
 
 
-@pytest.mark.parametrize("slots", [1024, 1 << 16])
-def test_extend_refill_keeps_results(ctx, slots):
-    """Extend with per-lane refill: hits, paths, accumulation and ray counts unchanged (and equal
-    the oracle), with a pool smaller than the frame and one larger."""
-    s = icospheres()
-    try:
-        ctx.configure_engine(slots=slots)
-        ctx.set_engine_drain(0)          # keep the step kernels running to the end
-        base, p = render(ctx, s, 3, size=(64, 36))
-        ctx.set_engine_refill(True)
-        got, _ = render(ctx, s, 3, size=(64, 36))
-    finally:
-        ctx.set_engine_refill(False)
-        ctx.set_engine_drain(1 << 22)
-        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
-                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
-    assert same_bits(got["paths"], base["paths"])
-    assert same_bits(got["accum"], base["accum"])
-    assert got["counters"][1:] == base["counters"][1:]
-    ref_acc, _, _ = oracle.render(s.view(), p, 0, 3, want_paths=False)
-    assert same_bits(got["accum"], ref_acc)
-
-
 @pytest.mark.parametrize("drain", [0, 1 << 10, 1 << 24])
 def test_drain_threshold_keeps_results(ctx, drain):
     """The run's switch to the one-kernel drain (never, late, or from the first step) changes
