@@ -459,8 +459,8 @@ lf_status lf_guide_train_device(lf_guide* g, const float* d_samples, int32_t n, 
 lf_status lf_guide_eval(lf_guide* g, const float* queries, int32_t n, float* mix, float* pdf);
 /* The guide's MLP on the tcgen05 tensor cores (1): inference (lf_guide_eval, guided
  * rendering) and training (lf_guide_train*, lf_guide_gradients) in 128-sample tiles, FP16
- * operands from shared memory, FP32 accumulators in tensor memory; or the warp-level mma.sync
- * kernels (0, default). Same encoding and FP16 roundings; the FP32 sums differ only in
+ * operands from shared memory, FP32 accumulators in tensor memory (default); or the warp-level
+ * mma.sync kernels (0). Same encoding and FP16 roundings; the FP32 sums differ only in
  * summation order. */
 lf_status lf_guide_set_tensor_path(lf_guide* g, int32_t tcgen05);
 /* Guided rendering of a frame (g = NULL detaches): at every surface hit a direction comes from

@@ -513,7 +513,7 @@ struct lf_guide
     Net net{};
     int step = 0;
     float lr = 1e-2f;
-    int tensorPath = 0;             // inference on tcgen05 (1) or warp-level mma.sync (0)
+    int tensorPath = 1;             // MLP on tcgen05 (1, default) or warp-level mma.sync (0)
 };
 
 namespace guidehost

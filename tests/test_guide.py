@@ -107,6 +107,7 @@ def test_device_pdf_matches_oracle(ctx):
     gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1])
     try:
         gd.set_params(wflat, gflat)
+        gd.set_tensor_path(False)      # the warp-level kernel; tcgen05 has its own test below
         mix, pdf = gd.eval(records(p, wo, nrm, wd, w))
     finally:
         gd.close()
@@ -161,6 +162,7 @@ def test_tcgen05_inference_matches_warp_mma_and_oracle(ctx, n):
     gd = lf.Guide(ctx, [0, 0, 0], [1, 1, 1])
     try:
         gd.set_params(wflat, gflat)
+        gd.set_tensor_path(False)
         mix_w, pdf_w = gd.eval(rec)
         gd.set_tensor_path(True)
         mix_t, pdf_t = gd.eval(rec)
