@@ -524,11 +524,17 @@ __device__ __noinline__ uint32_t mesh_binary(const DevScene S, int rootCode, int
     return err;
 }
 
-__device__ __forceinline__ void sort2(uint32_t& a, uint32_t& b)
+// Compare-exchange of two (key, child code) pairs by key: the codes travel with their keys, so
+// no per-slot lookup is needed after the sort.
+__device__ __forceinline__ void sort2(uint32_t& a, uint32_t& b, int& ca, int& cb)
 {
-    const uint32_t lo = min(a, b), hi = max(a, b);
+    const bool swap = b < a;
+    const uint32_t lo = swap ? b : a, hi = swap ? a : b;
+    const int clo = swap ? cb : ca, chi = swap ? ca : cb;
     a = lo;
     b = hi;
+    ca = clo;
+    cb = chi;
 }
 
 // Child hits of one wide node, nearest entry first: hc[0..nh). The children are ordered by a
@@ -554,6 +560,7 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
             g[q][h4 * 4 + 3] = f.w;
         }
     uint32_t key[kWide];
+    int child[kWide];
     int nh = 0;
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
@@ -566,37 +573,32 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
         const float e = fmaxf(t0, 0.f);
         const bool hit = t1 >= t0 && t1 > 0.f && e <= lim;
         key[j] = hit ? ((__float_as_uint(e) & ~kSlotMask) | (uint32_t)j) : 0xFFFFFFFFu;
+        child[j] = __float_as_int(g[6][j]);
         nh += hit ? 1 : 0;
     }
+#define LF_S2(a, b) sort2(key[a], key[b], child[a], child[b])
     if constexpr (kWide == 4)
     {
-        sort2(key[0], key[1]);
-        sort2(key[2], key[3]);
-        sort2(key[0], key[2]);
-        sort2(key[1], key[3]);
-        sort2(key[1], key[2]);
+        LF_S2(0, 1);
+        LF_S2(2, 3);
+        LF_S2(0, 2);
+        LF_S2(1, 3);
+        LF_S2(1, 2);
     }
     else
     {
         // Batcher's odd-even merge sort of 8
 #pragma unroll
-        for (int a = 0; a < 8; a += 2) sort2(key[a], key[a + 1]);
-        sort2(key[0], key[2]); sort2(key[1], key[3]); sort2(key[4], key[6]); sort2(key[5], key[7]);
-        sort2(key[1], key[2]); sort2(key[5], key[6]);
-        sort2(key[0], key[4]); sort2(key[1], key[5]); sort2(key[2], key[6]); sort2(key[3], key[7]);
-        sort2(key[2], key[4]); sort2(key[3], key[5]);
-        sort2(key[1], key[2]); sort2(key[3], key[4]); sort2(key[5], key[6]);
+        for (int a = 0; a < 8; a += 2) LF_S2(a, a + 1);
+        LF_S2(0, 2); LF_S2(1, 3); LF_S2(4, 6); LF_S2(5, 7);
+        LF_S2(1, 2); LF_S2(5, 6);
+        LF_S2(0, 4); LF_S2(1, 5); LF_S2(2, 6); LF_S2(3, 7);
+        LF_S2(2, 4); LF_S2(3, 5);
+        LF_S2(1, 2); LF_S2(3, 4); LF_S2(5, 6);
     }
+#undef LF_S2
 #pragma unroll
-    for (int k = 0; k < kWide; ++k)
-    {
-        const uint32_t slot = key[k] & kSlotMask;
-        int c = __float_as_int(g[6][0]);
-#pragma unroll
-        for (int j = 1; j < kWide; ++j)
-            if (slot == (uint32_t)j) c = __float_as_int(g[6][j]);
-        hc[k] = c;
-    }
+    for (int k = 0; k < kWide; ++k) hc[k] = child[k];
     return nh;
 }
 
