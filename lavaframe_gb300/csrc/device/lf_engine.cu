@@ -14,46 +14,29 @@ namespace
 __device__ __forceinline__ int job_of(int w) { return (int)((unsigned)w >> kPassRingBits); }
 __device__ __forceinline__ int ring_of(int w) { return w & (kPassRing - 1); }
 
-// Pass completion counting: warp leaders add into a small shared table keyed by ring
-// entry, then one global atomic per distinct entry of the block. Every thread must call.
+// Pass completion counts of a block: a small shared table keyed by ring entry, added into
+// passDone once per block at its end (an entry that finds the table full goes straight to the
+// global counter).
 struct DoneTable
 {
     int key[8];
     unsigned cnt[8];
 };
 
-__device__ __forceinline__ void count_done_block(int ring, unsigned long long* passDone, DoneTable& t)
+__device__ __forceinline__ void done_table_add(DoneTable& t, int ring, unsigned c, unsigned long long* passDone)
 {
-    if (threadIdx.x < 8)
+    if (ring < 0 || c == 0) return;
+    for (int k = 0; k < 8; ++k)
     {
-        t.key[threadIdx.x] = -1;
-        t.cnt[threadIdx.x] = 0;
-    }
-    __syncthreads();
-    const unsigned act = __ballot_sync(kFull, ring >= 0);
-    if (ring >= 0)
-    {
-        const unsigned peers = __match_any_sync(act, ring);
-        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        const int e = (ring + k) & 7;
+        const int old = atomicCAS(&t.key[e], -1, ring);
+        if (old == -1 || old == ring)
         {
-            bool placed = false;
-            for (int k = 0; k < 8 && !placed; ++k)
-            {
-                const int e = (ring + k) & 7;
-                const int old = atomicCAS(&t.key[e], -1, ring);
-                if (old == -1 || old == ring)
-                {
-                    atomicAdd(&t.cnt[e], (unsigned)__popc(peers));
-                    placed = true;
-                }
-            }
-            if (!placed) atomicAdd(&passDone[ring], (unsigned long long)__popc(peers));
+            atomicAdd(&t.cnt[e], c);
+            return;
         }
     }
-    __syncthreads();
-    if (threadIdx.x < 8 && t.key[threadIdx.x] >= 0 && t.cnt[threadIdx.x])
-        atomicAdd(&passDone[t.key[threadIdx.x]], (unsigned long long)t.cnt[threadIdx.x]);
-    __syncthreads();
+    atomicAdd(&passDone[ring], (unsigned long long)c);
 }
 
 // Largest pass g in [lo, hi) with pathBase <= id (passes are in increasing pathBase order).
@@ -127,50 +110,115 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
 }
 
 // ------------------------------------------------------------------ finish / refill
+constexpr int kFinishUnroll = 4;   // done entries a thread has in flight
+constexpr int kRefillBlock = 256;  // refill block size (8 warps)
+constexpr int kRefillGroups = 4;   // groups of kRefillBlock slots a refill block takes per round
+
 // Writes out the radiance of every path that finished in the previous step (counting pass
-// completions) and frees its slot.
-__global__ void engine_finish_kernel(EngineBuffers b, int parity)
+// completions) and frees its slot. A thread loads four entries' state before it writes any,
+// counts completions per run of equal ring entries, and the block adds its counts into the
+// global counters once, at its end: no block barrier inside the loop.
+__global__ void __launch_bounds__(256) engine_finish_kernel(EngineBuffers b, int parity)
 {
     __shared__ DoneTable table;
+    __shared__ unsigned blockWritten;
+    if (threadIdx.x < 8)
+    {
+        table.key[threadIdx.x] = -1;
+        table.cnt[threadIdx.x] = 0;
+    }
+    if (threadIdx.x == 0) blockWritten = 0;
+    __syncthreads();
     EngineCtl* ctl = b.ctl;
     const int n = ctl->doneCount[parity];
     const int* done = b.done[parity];
-    const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride)   // block-uniform
+    int run = -1;
+    unsigned runCount = 0, written = 0;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kFinishUnroll * stride)
     {
-        const int i = base + threadIdx.x;
-        const int slot = i < n ? done[i] : -1;
-        int ring = -1;
-        if (slot >= 0)
+        int slot[kFinishUnroll];
+        int4 inf[kFinishUnroll];
+        float4 L[kFinishUnroll];
+#pragma unroll
+        for (int u = 0; u < kFinishUnroll; ++u)
         {
-            int* info = reinterpret_cast<int*>(b.ps.info) + 4 * slot;
-            ring = ring_of(info[3]);
-            b.passes[ring].radiance[info[0]] = b.ps.L[slot];
-            info[3] = -1;
+            const int i = i0 + u * stride;
+            slot[u] = i < n ? done[i] : -1;
         }
-        count_done_block(ring, b.passDone, table);
-        const int written = __popc(__ballot_sync(kFull, ring >= 0));
-        if (lane == 0 && written)
-        {
-            atomicSub(&ctl->active, written);
-            atomicAdd(&ctl->freeCount, written);
-        }
+#pragma unroll
+        for (int u = 0; u < kFinishUnroll; ++u)
+            if (slot[u] >= 0)
+            {
+                inf[u] = b.ps.info[slot[u]];
+                L[u] = b.ps.L[slot[u]];
+            }
+#pragma unroll
+        for (int u = 0; u < kFinishUnroll; ++u)
+            if (slot[u] >= 0)
+            {
+                const int ring = ring_of(inf[u].w);
+                b.passes[ring].radiance[inf[u].x] = L[u];
+                reinterpret_cast<int*>(b.ps.info)[4 * slot[u] + 3] = -1;
+                if (ring != run)
+                {
+                    done_table_add(table, run, runCount, b.passDone);
+                    run = ring;
+                    runCount = 0;
+                }
+                ++runCount;
+                ++written;
+            }
+    }
+    done_table_add(table, run, runCount, b.passDone);
+    written = __reduce_add_sync(kFull, written);
+    if ((threadIdx.x & 31) == 0 && written) atomicAdd(&blockWritten, written);
+    __syncthreads();
+    if (threadIdx.x < 8 && table.key[threadIdx.x] >= 0 && table.cnt[threadIdx.x])
+        atomicAdd(&b.passDone[table.key[threadIdx.x]], (unsigned long long)table.cnt[threadIdx.x]);
+    if (threadIdx.x == 0 && blockWritten)
+    {
+        atomicSub(&ctl->active, (int)blockWritten);
+        atomicAdd(&ctl->freeCount, (int)blockWritten);
     }
 }
 
-// Starts min(free slots, unissued ids) new paths in free slots taken in slot order: the pool is
-// scanned block by block, a block's free slots get consecutive ids (next + k for the k-th slot
-// handed out), each new path gets its camera ray (renderer.glsl:27-62) and is queued for
-// extension (a depth-0 job's paths go straight to the done list with zero radiance). Handing
-// out slots in slot order keeps the paths a warp shades in neighbouring slots, so their state
-// comes in few cache lines, however the earlier paths finished.
-template <bool kOne>
-__global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
+// Exclusive scan of one int per lane; returns the warp total. All 32 lanes must call.
+__device__ __forceinline__ int warp_exclusive_scan(int& v)
 {
-    __shared__ int smem[33];
-    __shared__ int warpFree[32];
-    __shared__ int blockBase, blockDone;
+    const int lane = threadIdx.x & 31;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const int u = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += u;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    v = incl - v;
+    return total;
+}
+
+// Starts min(free slots, unissued ids) new paths in free slots taken in slot order: the pool is
+// scanned in rounds of kRefillGroups x kRefillBlock slots per block, a round's free slots get
+// consecutive ids (next + k for the k-th slot handed out, in slot order), each new path gets
+// its camera ray (renderer.glsl:27-62) and is queued for extension in the same order (a
+// depth-0 job's paths go straight to the done list with zero radiance). Handing out slots in
+// slot order keeps the paths a warp shades in neighbouring slots, so their state comes in few
+// cache lines, however the earlier paths finished. One round takes two block barriers (four
+// for a multi-job pool) and one atomic per counter.
+template <bool kOne>
+__global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
+{
+    constexpr int kG = kRefillGroups;
+    constexpr int kW = kRefillBlock / 32;
+    static_assert(kG * kW == 32, "one scan entry per lane of a warp");
+    // double-buffered by round, so that a round needs no barrier at its end
+    __shared__ unsigned freeMask[2][32];   // per (group, warp): free slots, then
+    __shared__ int freeOff[2][32];         // their exclusive offsets in the round
+    __shared__ int runOff[2][2][32];       // multi-job pool: queued / done offsets per (group, warp)
+    __shared__ unsigned runMask[2][2][32];
+    __shared__ int roundBase[2], queueBase[2], doneBase[2];
     EngineCtl* ctl = b.ctl;
     const unsigned long long next = ctl->next, total = ctl->total;
     const int freeCount = ctl->freeCount;
@@ -179,58 +227,132 @@ __global__ void engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
     if (m <= 0) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->taken = m;
     const unsigned long long plo = ctl->passLo, phi = ctl->numPasses;
-    const int stride = gridDim.x * blockDim.x;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int base = blockIdx.x * blockDim.x; base < b.cap; base += stride)   // block-uniform
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int* infoW = reinterpret_cast<const int*>(b.ps.info) + 3;
+    constexpr int kRound = kG * kRefillBlock;
+    int buf = 0;
+    for (int base = blockIdx.x * kRound; base < b.cap; base += gridDim.x * kRound, buf ^= 1)   // block-uniform
     {
-        const int cand = base + threadIdx.x;
-        const bool isFree = cand < b.cap && reinterpret_cast<const int*>(b.ps.info)[4 * cand + 3] == -1;
-        // rank of this free slot in the block, and the block's first id offset
-        const unsigned fm = __ballot_sync(kFull, isFree);
-        if (lane == 0) warpFree[warp] = __popc(fm);
-        __syncthreads();
-        if (threadIdx.x == 0)
+        bool isFree[kG];
+#pragma unroll
+        for (int g = 0; g < kG; ++g)
         {
-            int tot = 0;
-            for (int w = 0; w < nw; ++w)
+            const int cand = base + g * kRefillBlock + threadIdx.x;
+            isFree[g] = cand < b.cap && infoW[4 * (size_t)cand] == -1;
+        }
+#pragma unroll
+        for (int g = 0; g < kG; ++g)
+        {
+            const unsigned fm = __ballot_sync(kFull, isFree[g]);
+            if (lane == 0) freeMask[buf][g * kW + warp] = fm;
+        }
+        __syncthreads();
+        if (warp == 0)
+        {
+            int off = __popc(freeMask[buf][lane]);
+            const int tot = warp_exclusive_scan(off);
+            freeOff[buf][lane] = off;
+            if (lane == 0)
             {
-                const int c = warpFree[w];
-                warpFree[w] = tot;
-                tot += c;
+                // ids handed out so far: this round's share, or a look at the counter
+                const int rb = atomicAdd(&ctl->refillNext, tot);
+                roundBase[buf] = rb;
+                if constexpr (kOne)
+                {
+                    const int got = rb < m ? (tot < m - rb ? tot : m - rb) : 0;
+                    if (got)
+                        queueBase[buf] = atomicAdd(one.P.maxDepth > 0 ? &ctl->count[parity] : &ctl->doneCount[parity ^ 1],
+                                                   got);
+                }
             }
-            // ids handed out so far: this block's share, or a look at the counter
-            blockBase = atomicAdd(&ctl->refillNext, tot);
-            blockDone = blockBase >= m;
         }
         __syncthreads();
-        const int k = blockBase + warpFree[warp] + __popc(fm & ((1u << lane) - 1u));
-        const bool stop = blockDone;
-        __syncthreads();
-        if (stop) break;   // every id of this step is handed out
-        int slot = -1;
-        bool run = false;
-        if (isFree && k < m)
+        const int rb = roundBase[buf];
+        if (rb >= m) break;   // every id of this step is handed out
+        int slotOf[kG];
+        unsigned runBits = 0;
+#pragma unroll 1
+        for (int g = 0; g < kG; ++g)
         {
-            slot = cand;
-            const unsigned long long id = next + (unsigned long long)k;
-            const unsigned long long g = find_pass(b.passes, id, plo, phi);
-            const int r = (int)(g & (kPassRing - 1));
-            const EnginePass& Q = b.passes[r];
-            const Params& P = kOne ? one.P : b.jobs[Q.job].P;
-            const int local = (int)(id - Q.pathBase);   // passes hold < 2^31 paths
-            const int visPix = Q.visW * Q.visH;
-            const int s = local / visPix;
-            const int lp = local - s * visPix;
-            int lx, ly;
-            pixel_of(lp, Q.visW, Q.visH, lx, ly);
-            b.ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-            // x: the path's entry of the pass's [sample][visible pixel] radiance
-            b.ps.info[slot] = make_int4(s * visPix + ly * Q.visW + lx, 0, 0, r | (Q.job << kPassRingBits));
-            gen_path(P, Q.tileX, Q.tileY, Q.tileOrdinal, Q.firstSample + s, lx, ly, b.ps, slot);
-            run = P.maxDepth > 0;
+            slotOf[g] = -1;
+            const unsigned fm = freeMask[buf][g * kW + warp];
+            const int r = freeOff[buf][g * kW + warp] + __popc(fm & below);   // rank in the round
+            const int k = rb + r;
+            if (((fm >> lane) & 1u) && k < m)
+            {
+                const int slot = base + g * kRefillBlock + threadIdx.x;
+                const unsigned long long id = next + (unsigned long long)k;
+                const unsigned long long gp = find_pass(b.passes, id, plo, phi);
+                const int ring = (int)(gp & (kPassRing - 1));
+                const EnginePass& Q = b.passes[ring];
+                const Params& P = kOne ? one.P : b.jobs[Q.job].P;
+                const int local = (int)(id - Q.pathBase);   // passes hold < 2^31 paths
+                const int visPix = Q.visW * Q.visH;
+                const int s = local / visPix;
+                const int lp = local - s * visPix;
+                int lx, ly;
+                pixel_of(lp, Q.visW, Q.visH, lx, ly);
+                b.ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                // x: the path's entry of the pass's [sample][visible pixel] radiance
+                b.ps.info[slot] = make_int4(s * visPix + ly * Q.visW + lx, 0, 0, ring | (Q.job << kPassRingBits));
+                gen_path(P, Q.tileX, Q.tileY, Q.tileOrdinal, Q.firstSample + s, lx, ly, b.ps, slot);
+                if constexpr (kOne)
+                {
+                    // a single job's paths all go one way, in rank order
+                    int* dst = one.P.maxDepth > 0 ? b.queue[parity] : b.done[parity ^ 1];
+                    const int pos = queueBase[buf] + r;
+                    if (pos < b.cap) dst[pos] = slot;
+                    else set_error(b.status, LF_DEVERR_QUEUE);
+                }
+                else
+                {
+                    slotOf[g] = slot;
+                    if (P.maxDepth > 0) runBits |= 1u << g;
+                }
+            }
         }
-        block_push(run, slot, b.queue[parity], &ctl->count[parity], b.cap, b.status, smem);
-        block_push(slot >= 0 && !run, slot, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status, smem);
+        if constexpr (!kOne)
+        {
+            // jobs of different depths: queued and done paths ranked in slot order
+#pragma unroll
+            for (int g = 0; g < kG; ++g)
+            {
+                const unsigned qm = __ballot_sync(kFull, slotOf[g] >= 0 && ((runBits >> g) & 1u));
+                const unsigned dm = __ballot_sync(kFull, slotOf[g] >= 0 && !((runBits >> g) & 1u));
+                if (lane == 0)
+                {
+                    runMask[buf][0][g * kW + warp] = qm;
+                    runMask[buf][1][g * kW + warp] = dm;
+                }
+            }
+            __syncthreads();
+            if (warp == 0)
+            {
+                int qo = __popc(runMask[buf][0][lane]), dn = __popc(runMask[buf][1][lane]);
+                const int qt = warp_exclusive_scan(qo), dt = warp_exclusive_scan(dn);
+                runOff[buf][0][lane] = qo;
+                runOff[buf][1][lane] = dn;
+                if (lane == 0)
+                {
+                    queueBase[buf] = qt ? atomicAdd(&ctl->count[parity], qt) : 0;
+                    doneBase[buf] = dt ? atomicAdd(&ctl->doneCount[parity ^ 1], dt) : 0;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int g = 0; g < kG; ++g)
+            {
+                if (slotOf[g] < 0) continue;
+                const int q = ((runBits >> g) & 1u) ? 0 : 1;
+                const int e = g * kW + warp;
+                const int pos = (q ? doneBase[buf] : queueBase[buf]) + runOff[buf][q][e] +
+                                __popc(runMask[buf][q][e] & below);
+                int* dst = q ? b.done[parity ^ 1] : b.queue[parity];
+                if (pos < b.cap) dst[pos] = slotOf[g];
+                else set_error(b.status, LF_DEVERR_QUEUE);
+            }
+        }
     }
 }
 
@@ -547,8 +669,9 @@ void step(const EngineBuffers& b, const EngineJob& one, int parity, cudaStream_t
 {
     const int BF = 256;
     engine_finish_kernel<<<full_grid((const void*)engine_finish_kernel, BF, b.cap), BF, 0, st>>>(b, parity);
-    engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, BF, b.cap), BF, 0, st>>>(b, one,
-                                                                                                          parity);
+    engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, kRefillBlock,
+                                           (long long)b.cap / kRefillGroups),
+                                 kRefillBlock, 0, st>>>(b, one, parity);
     engine_reset_kernel<<<1, 1, 0, st>>>(b.ctl, parity);
     const int be = b.blockExtend > 0 ? b.blockExtend : 128;
     const int bs = b.blockShade > 0 ? b.blockShade : 128;
@@ -584,8 +707,9 @@ void drain_step(const EngineBuffers& b, const EngineJob& one, cudaStream_t st)
     for (int parity = 0; parity < 2; ++parity)
     {
         engine_finish_kernel<<<full_grid((const void*)engine_finish_kernel, BF, b.cap), BF, 0, st>>>(b, parity);
-        engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, BF, b.cap), BF, 0, st>>>(
-            b, one, parity);
+        engine_refill_kernel<kOne><<<full_grid((const void*)engine_refill_kernel<kOne>, kRefillBlock,
+                                               (long long)b.cap / kRefillGroups),
+                                     kRefillBlock, 0, st>>>(b, one, parity);
         engine_reset_kernel<<<1, 1, 0, st>>>(b.ctl, parity);
         engine_drain_kernel<kOne><<<full_grid((const void*)engine_drain_kernel<kOne>, 128, b.cap), 128, 0, st>>>(
             b, one, parity);
