@@ -39,6 +39,66 @@ __device__ __forceinline__ void done_table_add(DoneTable& t, int ring, unsigned 
     atomicAdd(&passDone[ring], (unsigned long long)c);
 }
 
+// Per-block completion bookkeeping of the kernels that end paths (finish, shade, shadow,
+// drain): completions summed per thread while the ring entry repeats, per block in a shared
+// table, and into the global counters once per block at its end.
+struct BlockDone
+{
+    DoneTable table;
+    unsigned written;
+};
+
+__device__ __forceinline__ void block_done_begin(BlockDone& bd)
+{
+    if (threadIdx.x < 8)
+    {
+        bd.table.key[threadIdx.x] = -1;
+        bd.table.cnt[threadIdx.x] = 0;
+    }
+    if (threadIdx.x == 0) bd.written = 0;
+    __syncthreads();
+}
+
+struct ThreadDone
+{
+    int run = -1;
+    unsigned runCount = 0, written = 0;
+};
+
+// Writes out the final radiance L of the path in `slot` into its pass's buffer, frees the slot
+// and counts the completion.
+__device__ __forceinline__ void end_path(const EngineBuffers& b, int slot, const int4& inf, const float4& L,
+                                         ThreadDone& td, BlockDone& bd)
+{
+    const int ring = ring_of(inf.w);
+    b.passes[ring].radiance[inf.x] = L;
+    reinterpret_cast<int*>(b.ps.info)[4 * slot + 3] = -1;
+    if (ring != td.run)
+    {
+        done_table_add(bd.table, td.run, td.runCount, b.passDone);
+        td.run = ring;
+        td.runCount = 0;
+    }
+    ++td.runCount;
+    ++td.written;
+}
+
+// Every thread of the block must call, once, after its last end_path.
+__device__ __forceinline__ void block_done_end(const EngineBuffers& b, const ThreadDone& td, BlockDone& bd)
+{
+    done_table_add(bd.table, td.run, td.runCount, b.passDone);
+    const unsigned w = __reduce_add_sync(kFull, td.written);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&bd.written, w);
+    __syncthreads();
+    if (threadIdx.x < 8 && bd.table.key[threadIdx.x] >= 0 && bd.table.cnt[threadIdx.x])
+        atomicAdd(&b.passDone[bd.table.key[threadIdx.x]], (unsigned long long)bd.table.cnt[threadIdx.x]);
+    if (threadIdx.x == 0 && bd.written)
+    {
+        atomicSub(&b.ctl->active, (int)bd.written);
+        atomicAdd(&b.ctl->freeCount, (int)bd.written);
+    }
+}
+
 // Largest pass g in [lo, hi) with pathBase <= id (passes are in increasing pathBase order).
 __device__ __forceinline__ unsigned long long find_pass(const EnginePass* passes, unsigned long long id,
                                                         unsigned long long lo, unsigned long long hi)
@@ -114,27 +174,17 @@ constexpr int kFinishUnroll = 4;   // done entries a thread has in flight
 constexpr int kRefillBlock = 256;  // refill block size (8 warps)
 constexpr int kRefillGroups = 4;   // groups of kRefillBlock slots a refill block takes per round
 
-// Writes out the radiance of every path that finished in the previous step (counting pass
-// completions) and frees its slot. A thread loads four entries' state before it writes any,
-// counts completions per run of equal ring entries, and the block adds its counts into the
-// global counters once, at its end: no block barrier inside the loop.
+// Writes out the radiance of the paths on the done list (paths of depth-0 jobs; the step
+// kernels end every other path where it ends), counting pass completions, and frees their
+// slots. A thread loads four entries' state before it writes any.
 __global__ void __launch_bounds__(256) engine_finish_kernel(EngineBuffers b, int parity)
 {
-    __shared__ DoneTable table;
-    __shared__ unsigned blockWritten;
-    if (threadIdx.x < 8)
-    {
-        table.key[threadIdx.x] = -1;
-        table.cnt[threadIdx.x] = 0;
-    }
-    if (threadIdx.x == 0) blockWritten = 0;
-    __syncthreads();
-    EngineCtl* ctl = b.ctl;
-    const int n = ctl->doneCount[parity];
+    __shared__ BlockDone bd;
+    block_done_begin(bd);
+    ThreadDone td;
+    const int n = b.ctl->doneCount[parity];
     const int* done = b.done[parity];
     const int stride = gridDim.x * blockDim.x;
-    int run = -1;
-    unsigned runCount = 0, written = 0;
     for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kFinishUnroll * stride)
     {
         int slot[kFinishUnroll];
@@ -155,32 +205,9 @@ __global__ void __launch_bounds__(256) engine_finish_kernel(EngineBuffers b, int
             }
 #pragma unroll
         for (int u = 0; u < kFinishUnroll; ++u)
-            if (slot[u] >= 0)
-            {
-                const int ring = ring_of(inf[u].w);
-                b.passes[ring].radiance[inf[u].x] = L[u];
-                reinterpret_cast<int*>(b.ps.info)[4 * slot[u] + 3] = -1;
-                if (ring != run)
-                {
-                    done_table_add(table, run, runCount, b.passDone);
-                    run = ring;
-                    runCount = 0;
-                }
-                ++runCount;
-                ++written;
-            }
+            if (slot[u] >= 0) end_path(b, slot[u], inf[u], L[u], td, bd);
     }
-    done_table_add(table, run, runCount, b.passDone);
-    written = __reduce_add_sync(kFull, written);
-    if ((threadIdx.x & 31) == 0 && written) atomicAdd(&blockWritten, written);
-    __syncthreads();
-    if (threadIdx.x < 8 && table.key[threadIdx.x] >= 0 && table.cnt[threadIdx.x])
-        atomicAdd(&b.passDone[table.key[threadIdx.x]], (unsigned long long)table.cnt[threadIdx.x]);
-    if (threadIdx.x == 0 && blockWritten)
-    {
-        atomicSub(&ctl->active, (int)blockWritten);
-        atomicAdd(&ctl->freeCount, (int)blockWritten);
-    }
+    block_done_end(b, td, bd);
 }
 
 // Exclusive scan of one int per lane; returns the warp total. All 32 lanes must call.
@@ -451,6 +478,9 @@ template <bool kOne, int kThreadsPerSm, bool kLights = true>
 __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
     engine_shade_kernel(EngineBuffers b, EngineJob one, int parity)
 {
+    __shared__ BlockDone bd;
+    block_done_begin(bd);
+    ThreadDone td;
     EngineCtl* ctl = b.ctl;
     const int n = ctl->count[parity];
     const int nHit = ctl->hitCount;   // part: hits at [0, nHit), misses at the back
@@ -465,7 +495,7 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const int i = base + lane;
-        bool pushExt = false, pushShadow = false, finished = false;
+        bool pushExt = false, pushShadow = false;
         int p = -1;
         ShadowRec rec;
         if (i < n)
@@ -489,18 +519,50 @@ __global__ void __launch_bounds__(256, kThreadsPerSm ? kThreadsPerSm / 256 : 1)
                 const EngineJob& J = b.jobs[job_of(w)];
                 shade_path(J.S, J.P, b.ps, p, b.ctr, pushExt, pushShadow, rec);
             }
-            finished = !pushExt;
+            // a path that ends here is written out now, or by the shadow kernel after its
+            // next-event rays
+            if (!pushExt && pushShadow) rec.b.w = __uint_as_float(__float_as_uint(rec.b.w) | 4u);
+            else if (!pushExt) end_path(b, p, b.ps.info[p], b.ps.L[p], td, bd);
         }
         __syncwarp();
         warp_push(pushExt, p, qout, &ctl->count[parity ^ 1], b.cap, b.status);
-        warp_push(pushShadow, rec, b.shadow, &ctl->shadowCount, b.cap, b.status);
-        warp_push(finished, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status);
+        if constexpr (kLights)
+            warp_push(pushShadow, rec, b.shadow, &ctl->shadowCount, b.cap, b.status);
+        else
+        {
+            // no light rays: the record's light fields are never read, so they are not written
+            const unsigned m = __ballot_sync(kFull, pushShadow);
+            if (m)
+            {
+                int base = 0;
+                if (lane == __ffs(m) - 1) base = atomicAdd(&ctl->shadowCount, __popc(m));
+                base = __shfl_sync(kFull, base, __ffs(m) - 1);
+                if (pushShadow)
+                {
+                    const int pos = base + __popc(m & ((1u << lane) - 1u));
+                    if (pos < b.cap)
+                    {
+                        ShadowRec* r = b.shadow + pos;
+                        r->a = rec.a;
+                        r->b = rec.b;
+                        r->c = rec.c;
+                        r->e = rec.e;
+                    }
+                    else
+                        set_error(b.status, LF_DEVERR_QUEUE);
+                }
+            }
+        }
     }
+    block_done_end(b, td, bd);
 }
 
 template <bool kOne>
 __global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob one)
 {
+    __shared__ BlockDone bd;
+    block_done_begin(bd);
+    ThreadDone td;
     const int n = b.ctl->shadowCount;
     unsigned long long rays = 0;
     const int lane = threadIdx.x & 31;
@@ -513,23 +575,30 @@ __global__ void __maxnreg__(72) engine_shadow_kernel(EngineBuffers b, EngineJob 
         const int i = base + lane;
         if (i >= n) continue;
         const ShadowRec* rec = b.shadow + i;
+        float4 L;
         if constexpr (kOne)
-            set_error(b.status, shadow_path(one.S, one.P, b.ps, rec, rays));
+            set_error(b.status, shadow_path(one.S, one.P, b.ps, rec, rays, &L));
         else
         {
             const int p = __float_as_int(rec->a.w);
             const int w = reinterpret_cast<const int*>(b.ps.info)[4 * p + 3];
             const EngineJob& J = b.jobs[job_of(w)];
-            set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, rays));
+            set_error(b.status, shadow_path(J.S, J.P, b.ps, rec, rays, &L));
+        }
+        if (__float_as_uint(rec->b.w) & 4u)   // the path ended at this record's vertex
+        {
+            const int p = __float_as_int(rec->a.w);
+            end_path(b, p, b.ps.info[p], L, td, bd);
         }
     }
     warp_count_add(&b.ctr[2], rays);
+    block_done_end(b, td, bd);
 }
 
 // ------------------------------------------------------------------ drain
 // The last paths of a run, once no ids are left to issue: every queued path is taken through
 // its remaining bounces by one thread (extension, shade, next-event rays, in the order of the
-// step kernels) and queued as done. Per path this is the same sequence of operations the step
+// step kernels) and written out. Per path this is the same sequence of operations the step
 // kernels perform, so results and ray counts are unchanged; what goes away is one launch
 // sequence per bounce whose length is set by the slowest ray of an almost empty pool.
 // One path from its queued extension ray to its end; returns the extension and shadow rays
@@ -556,6 +625,9 @@ __device__ __forceinline__ void drain_path(const EngineBuffers& b, const EngineJ
 template <bool kOne>
 __global__ void __launch_bounds__(128) engine_drain_kernel(EngineBuffers b, EngineJob one, int parity)
 {
+    __shared__ BlockDone bd;
+    block_done_begin(bd);
+    ThreadDone td;
     EngineCtl* ctl = b.ctl;
     const int n = ctl->count[parity];
     const int* q = b.queue[parity];
@@ -568,20 +640,19 @@ __global__ void __launch_bounds__(128) engine_drain_kernel(EngineBuffers b, Engi
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const int i = base + lane;
-        int p = -1;
         if (i < n)
         {
-            p = q[i];
+            const int p = q[i];
             if constexpr (kOne)
                 drain_path(b, one, p, ext, shadowRays);
             else
                 drain_path(b, b.jobs[job_of(reinterpret_cast<const int*>(b.ps.info)[4 * p + 3])], p, ext, shadowRays);
+            end_path(b, p, b.ps.info[p], b.ps.L[p], td, bd);
         }
-        __syncwarp();
-        warp_push(p >= 0, p, b.done[parity ^ 1], &ctl->doneCount[parity ^ 1], b.cap, b.status);
     }
     warp_count_add(&b.ctr[1], ext);
     warp_count_add(&b.ctr[2], shadowRays);
+    block_done_end(b, td, bd);
 }
 
 // ------------------------------------------------------------------ accumulate

@@ -10,14 +10,17 @@
 // image sums are the ones of the per-batch pipeline, bit for bit.
 //
 // One engine step with parity k (graph-captured, two steps per graph so the parity returns):
-//   finish   done[k]: write out finished paths, count pass completions, free their slots
+//   finish   done[k] (paths of depth-0 jobs): write them out, count pass completions, free
+//            their slots
 //   refill   start new paths in free slots while unissued ids remain (-> queue[k])
 //   reset    commit the refill, clear done[k], the shadow queue and queue[k^1]
 //   extend   closest hit of every queued path; hits and misses -> part (front and back), or
 //            with sort-by-material the hits into one bucket per material class
 //   shade    one PathTrace bounce over part's hits, then its misses, so that a warp shades
-//            one kind; survivors -> queue[k^1], finished -> done[k^1]
-//   shadow   next-event visibility
+//            one kind; survivors -> queue[k^1]; a path that ends without next-event rays is
+//            written out (radiance into its pass, completion counted, slot freed) on the spot
+//   shadow   next-event visibility; writes out the paths that ended at the record's vertex
+//   (the drain kernel writes out each path it runs to its end)
 #pragma once
 
 #include "lf_kernels.h"
@@ -71,7 +74,7 @@ struct EngineBuffers
     int* partSort;               // sort-by-material: hits of class k at [k * cap, k * cap + bucketCount[k])
     int sortByMaterial;          // 1: extend buckets hits by material class, shade takes them class by class
     ShadowRec* shadow;
-    int* done[2];                // slots whose path finished
+    int* done[2];                // slots of depth-0 paths, written out by the next finish
     EngineCtl* ctl;
     const EngineJob* jobs;
     const EnginePass* passes;    // ring of kPassRing

@@ -25,7 +25,7 @@ struct PathSoA
 struct ShadowRec
 {
     float4 a;   // surface position, w: path slot (int bits)
-    float4 b;   // throughput, w: flags (1 env ray, 2 light ray)
+    float4 b;   // throughput, w: flags (1 env ray, 2 light ray; engine: 4 the path ends after these rays)
     float4 c;   // environment direction
     float4 e;   // environment contribution
     float4 f;   // light direction, w: max distance

@@ -440,8 +440,10 @@ __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P,
 // (pathtrace.glsl:126-204, 266). Returns device error bits; counts traced rays. The record is
 // read field by field where it is used (a queued record in global memory, or the drain's own),
 // so that only the position, the path, the flags and Li stay live across the traversals.
+// `Lout`, when given, receives the path's radiance as written.
 __device__ __forceinline__ uint32_t shadow_path(const ShadeScene& S, const Params& P, const PathSoA& ps,
-                                                const ShadowRec* rec, unsigned long long& rays)
+                                                const ShadowRec* rec, unsigned long long& rays,
+                                                float4* Lout = nullptr)
 {
     using namespace pathops;
     const bool lights = P.useLights != 0;
@@ -472,6 +474,7 @@ __device__ __forceinline__ uint32_t shadow_path(const ShadeScene& S, const Param
     float4 L4 = ps.L[p];
     v3 L = f3(L4) + Li * f3(T4);
     ps.L[p] = f4(L, 0.f);
+    if (Lout) *Lout = f4(L, 0.f);
     return err;
 }
 }
