@@ -199,19 +199,8 @@ __device__ __forceinline__ void encode_tile(const Net& net, const float* p, cons
     position01(net, p, p01);
     for (int l = h * 4; l < h * 4 + 4; ++l)
     {
-        uint32_t idx[8];
-        float w[8];
-        grid_corners(net.res[l], p01, idx, w);
-        const __half* tab = net.grid + (size_t)l * kT * kFeatures;
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int c = 0; c < 8; ++c)
-        {
-            const uint2 v = *reinterpret_cast<const uint2*>(tab + (size_t)idx[c] * kFeatures);
-            acc[0] += w[c] * lo_f(v.x);
-            acc[1] += w[c] * hi_f(v.x);
-            acc[2] += w[c] * lo_f(v.y);
-            acc[3] += w[c] * hi_f(v.y);
-        }
+        float acc[4];
+        level_features(net, l, p01, acc);
         for (int f = 0; f < 4; ++f) row[l * 4 + f] = __float2half(acc[f]);
     }
     const float* d = h == 0 ? wo : n;
@@ -435,12 +424,13 @@ __global__ void __launch_bounds__(kInferWarps * 32) guide_infer_kernel(Net net, 
                 e[i] = __expf(out[5 * i + 4] - mx);
                 es += e[i];
             }
+            const float invEs = 1.f / es;
             float cum = 0.f;
             for (int i = 0; i < kLobes; ++i)
             {
                 float mu[3], k;
                 lobe_params(out + 5 * i, mu, &k);
-                cum += e[i] / es;
+                cum += e[i] * invEs;
                 dst[5 * i + 0] = mu[0];
                 dst[5 * i + 1] = mu[1];
                 dst[5 * i + 2] = mu[2];

@@ -41,31 +41,80 @@ struct Net
     float invExt[3];
 };
 
-__device__ __forceinline__ uint32_t vertex_index(int res, uint32_t x, uint32_t y, uint32_t z)
-{
-    const uint32_t n = (uint32_t)res + 1u;
-    if ((unsigned long long)n * n * n <= (unsigned long long)kT) return x + y * n + z * n * n;
-    return ((x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u)) & (uint32_t)(kT - 1);
-}
-
-// Level l: the 8 corner entries and trilinear weights of position p01 in [0, 1]^3.
+// Level l: the 8 corner entries and trilinear weights of position p01 in [0, 1]^3 (corner c =
+// dx + 2 dy + 4 dz). A corner (x, y, z) of a level with n = res + 1 vertices per axis has the
+// dense entry x + y n + z n^2 while n^3 fits the table, else the spatial hash
+// (x * 1) ^ (y * 2654435761) ^ (z * 805459861) mod T (uint32 arithmetic); both are formed from
+// per-axis terms. The weights are (wx * wy) * wz.
 __device__ __forceinline__ void grid_corners(int res, const float p01[3], uint32_t idx[8], float w[8])
 {
-    int i0[3];
+    uint32_t i0[3];
     float fr[3];
+#pragma unroll
     for (int a = 0; a < 3; ++a)
     {
         const float q = fminf(fmaxf(p01[a], 0.f), 1.f) * (float)res;
         int i = (int)floorf(q);
         i = i > res - 1 ? res - 1 : i;
-        i0[a] = i;
+        i0[a] = (uint32_t)i;
         fr[a] = q - (float)i;
     }
+    const uint32_t n = (uint32_t)res + 1u;
+    uint32_t hx[2], hy[2], hz[2];
+    if ((unsigned long long)n * n * n <= (unsigned long long)kT)
+    {
+        // dense: x + y n + z n^2
+        hx[0] = i0[0];
+        hy[0] = i0[1] * n;
+        hz[0] = i0[2] * n * n;
+        hx[1] = hx[0] + 1u;
+        hy[1] = hy[0] + n;
+        hz[1] = hz[0] + n * n;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) idx[c] = hx[c & 1] + hy[(c >> 1) & 1] + hz[c >> 2];
+    }
+    else
+    {
+        // spatial hash: (x * 1) ^ (y * 2654435761) ^ (z * 805459861) mod T
+        hx[0] = i0[0];
+        hy[0] = i0[1] * 2654435761u;
+        hz[0] = i0[2] * 805459861u;
+        hx[1] = hx[0] + 1u;
+        hy[1] = hy[0] + 2654435761u;
+        hz[1] = hz[0] + 805459861u;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) idx[c] = (hx[c & 1] ^ hy[(c >> 1) & 1] ^ hz[c >> 2]) & (uint32_t)(kT - 1);
+    }
+    const float wx[2] = {1.f - fr[0], fr[0]}, wy[2] = {1.f - fr[1], fr[1]}, wz[2] = {1.f - fr[2], fr[2]};
+    float wxy[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) wxy[c] = wx[c & 1] * wy[c >> 1];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) w[c] = wxy[c & 3] * wz[c >> 2];
+}
+
+// The 4 features of level l at p01: trilinear sum of the corner entries (FP16 table, FP32
+// fused multiply-adds in corner order).
+__device__ __forceinline__ void level_features(const Net& net, int l, const float p01[3], float acc[4])
+{
+    uint32_t idx[8];
+    float w[8];
+    grid_corners(net.res[l], p01, idx, w);
+    const __half* tab = net.grid + (size_t)l * kT * kFeatures;
+    uint2 v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = *reinterpret_cast<const uint2*>(tab + (size_t)idx[c] * kFeatures);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) acc[f] = 0.f;
+#pragma unroll
     for (int c = 0; c < 8; ++c)
     {
-        const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
-        idx[c] = vertex_index(res, (uint32_t)(i0[0] + dx), (uint32_t)(i0[1] + dy), (uint32_t)(i0[2] + dz));
-        w[c] = (dx ? fr[0] : 1.f - fr[0]) * (dy ? fr[1] : 1.f - fr[1]) * (dz ? fr[2] : 1.f - fr[2]);
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v[c].x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&v[c].y));
+        acc[0] = __fmaf_rn(w[c], a.x, acc[0]);
+        acc[1] = __fmaf_rn(w[c], a.y, acc[1]);
+        acc[2] = __fmaf_rn(w[c], b.x, acc[2]);
+        acc[3] = __fmaf_rn(w[c], b.y, acc[3]);
     }
 }
 
@@ -90,7 +139,7 @@ __device__ __forceinline__ float grid_feature(const Net& net, const float p01[3]
     grid_corners(net.res[l], p01, idx, w);
     const __half* tab = net.grid + (size_t)l * kT * kFeatures;
     float acc = 0.f;
-    for (int c = 0; c < 8; ++c) acc += w[c] * __half2float(tab[idx[c] * kFeatures + f]);
+    for (int c = 0; c < 8; ++c) acc = __fmaf_rn(w[c], __half2float(tab[idx[c] * kFeatures + f]), acc);
     return acc;
 }
 
@@ -109,9 +158,10 @@ __device__ __forceinline__ void lobe_params(const float* o5, float mu[3], float*
     const float len = sqrtf(o5[0] * o5[0] + o5[1] * o5[1] + o5[2] * o5[2]);
     if (len > 1e-30f)
     {
-        mu[0] = o5[0] / len;
-        mu[1] = o5[1] / len;
-        mu[2] = o5[2] / len;
+        const float inv = 1.f / len;
+        mu[0] = o5[0] * inv;
+        mu[1] = o5[1] * inv;
+        mu[2] = o5[2] * inv;
     }
     else
     {
@@ -122,7 +172,7 @@ __device__ __forceinline__ void lobe_params(const float* o5, float mu[3], float*
     *kappa = __expf(fminf(fmaxf(o5[3], -3.f), 7.f));
 }
 
-__device__ __forceinline__ float vmf_norm(float k) { return k / (6.28318531f * (1.f - __expf(-2.f * k))); }
+__device__ __forceinline__ float vmf_norm(float k) { return __fdividef(k, 6.28318531f * (1.f - __expf(-2.f * k))); }
 
 // Mixture pdf from the compact per-query form (mu xyz, kappa, cumulative weight per lobe).
 __device__ __forceinline__ float mix_pdf(const float* mix, float wx, float wy, float wz)

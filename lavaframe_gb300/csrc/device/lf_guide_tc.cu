@@ -45,12 +45,17 @@ namespace guide
 namespace
 {
 constexpr int kTcRows = 128;                         // queries per tile = MMA M
-constexpr int kTcThreads = 128;                      // one thread per query
-constexpr uint32_t kTmemCols = 128;                  // two 64-column FP32 accumulators
+constexpr int kTcThreads = 128;                      // one thread per query (training)
 constexpr int kTileBytes = kTcRows * kIn * 2;        // A tile: 128 x 64 FP16
 constexpr int kLayerBytes = 64 * 64 * 2;             // W1..W3: 64 x 64 FP16
 constexpr int kWBytes = 3 * kLayerBytes + kOut * 64 * 2;
-constexpr int kTcSmem = kWBytes + kTileBytes + 16;   // + mbarrier and TMEM address
+// Inference: kInferGroups warpgroups per CTA, each running its own tiles through its own A tile,
+// 64 TMEM columns and mbarrier; the weights in shared memory are the CTA's, shared.
+constexpr int kInferGroups = 2;
+constexpr int kInferThreads = 128 * kInferGroups;
+constexpr int kInferCtasPerSm = 3;                   // 3 x 64 KB shared memory, 3 x 128 TMEM columns
+constexpr uint32_t kTmemCols = 64 * kInferGroups;
+constexpr int kTcSmem = kWBytes + kInferGroups * kTileBytes + 16 * kInferGroups;   // + per group mbarrier, TMEM address
 constexpr uint32_t kLbo = 128;                       // core matrices adjacent along K
 constexpr uint32_t kSbo = 1024;                      // adjacent 8-row groups (8 core matrices of K = 64)
 constexpr long long kWaitCycles = 4000000000LL;      // ~2 s at 2 GHz
@@ -135,6 +140,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// One FP32 accumulator column of this thread's TMEM lane.
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr)
+{
+    uint32_t r;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr));
+    return __uint_as_float(r);
+}
+
 __device__ __forceinline__ void store8(unsigned char* tile, int row, int k0, const float* v, int kg = 8)
 {
     __half2 h[4];
@@ -173,20 +186,8 @@ __device__ __forceinline__ void encode_row(const Net& net, const float* rec, boo
 #pragma unroll 1
         for (int l = 0; l < kLevels; ++l)
         {
-            uint32_t idx[8];
-            float w[8];
-            grid_corners(net.res[l], p01, idx, w);
-            const __half* tab = net.grid + (size_t)l * kT * kFeatures;
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int c = 0; c < 8; ++c)
-            {
-                const uint2 v = *reinterpret_cast<const uint2*>(tab + (size_t)idx[c] * kFeatures);
-                const __half2 a = *reinterpret_cast<const __half2*>(&v.x), b = *reinterpret_cast<const __half2*>(&v.y);
-                acc[0] += w[c] * __low2float(a);
-                acc[1] += w[c] * __high2float(a);
-                acc[2] += w[c] * __low2float(b);
-                acc[3] += w[c] * __high2float(b);
-            }
+            float acc[4];
+            level_features(net, l, p01, acc);
             // unrolled stores keep f[] in registers
 #pragma unroll
             for (int q = 0; q < kLevels; ++q)
@@ -215,22 +216,81 @@ __device__ __forceinline__ void encode_row(const Net& net, const float* rec, boo
 #pragma unroll
     for (int k0 = 0; k0 < 64; k0 += 8) store8(tile, row, k0, f + k0);
 }
+
+// Inference form of encode_row: the same FP16 values, written level by level (8 bytes at a
+// time) so that no 64-feature array stays live.
+__device__ __forceinline__ void encode_row_direct(const Net& net, const float* rec, bool valid, unsigned char* tile,
+                                                  int row)
+{
+    if (!valid)
+    {
+#pragma unroll
+        for (int k0 = 0; k0 < 64; k0 += 8) *reinterpret_cast<uint4*>(tile + cm_offset(row, k0)) = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    float p01[3];
+    position01(net, rec, p01);
+#pragma unroll 1
+    for (int l = 0; l < kLevels; ++l)
+    {
+        float acc[4];
+        level_features(net, l, p01, acc);
+        const __half2 h0 = __floats2half2_rn(acc[0], acc[1]), h1 = __floats2half2_rn(acc[2], acc[3]);
+        uint2 o;
+        o.x = *reinterpret_cast<const uint32_t*>(&h0);
+        o.y = *reinterpret_cast<const uint32_t*>(&h1);
+        *reinterpret_cast<uint2*>(tile + cm_offset(row, 4 * l)) = o;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+    {
+        const float* d = rec + 3 + 3 * h;   // outgoing direction, then the normal
+        float th, ph;
+        sph01(d[0], d[1], d[2], &th, &ph);
+        float f[8];
+#pragma unroll
+        for (int k = 0; k < kBlobBins; ++k) f[k] = blob(th, k);
+        store8(tile, row, 32 + h * 16, f);
+#pragma unroll
+        for (int k = 0; k < kBlobBins; ++k) f[k] = blob(ph, k);
+        store8(tile, row, 32 + h * 16 + 8, f);
+    }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+// Barrier of one warpgroup (named barrier id, 128 threads).
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+// Barrier of one warpgroup that returns whether any of its threads passed true.
+__device__ __forceinline__ bool group_sync_or(int id, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+}
+
+// kInferGroups warpgroups per CTA; warpgroup g takes tiles blockIdx.x * kInferGroups + g,
+// stepping by gridDim.x * kInferGroups, and synchronises on its own named barrier (1 + g), so
+// that one group's MMAs and waits overlap the other's encoding and epilogue.
+__global__ void __launch_bounds__(kInferThreads, kInferCtasPerSm)
     guide_infer_tc_kernel(Net net, const float* queries, int n, const int* nDev, float* mix, uint32_t* status)
 {
     if (nDev) n = *nDev;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sW = smem;
-    unsigned char* sA = smem + kWBytes;
-    uint64_t* mbarPtr = reinterpret_cast<uint64_t*>(smem + kWBytes + kTileBytes);
-    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(smem + kWBytes + kTileBytes + 8);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t mbar = smem_addr(mbarPtr);
+    const int grp = tid >> 7, row = tid & 127;
+    unsigned char* sW = smem;
+    unsigned char* sA = smem + kWBytes + grp * kTileBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kWBytes + kInferGroups * kTileBytes);
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(bars + kInferGroups);
+    const uint32_t mbar = smem_addr(bars + grp);
 
     // weights [out][in] of the four layers -> B operands in core-matrix layout
-    for (int i = tid; i < kWeights; i += kTcThreads)
+    for (int i = tid; i < kWeights; i += kInferThreads)
     {
         const int l = i < 3 * 4096 ? i >> 12 : 3;
         const int r = (i - l * 4096) >> 6, k = (i - l * 4096) & 63;
@@ -243,7 +303,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0)
+    if (row == 0)
     {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -252,83 +312,90 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    const uint32_t tmem = *tmemSlot;
-    const uint32_t lane0 = (uint32_t)(warp * 32) << 16;   // this warp's TMEM lane quarter
+    // the group's 64 accumulator columns; warp w reads TMEM lanes 32 (w % 4) .. + 31
+    const uint32_t acc = *tmemSlot + (uint32_t)(64 * grp);
+    const uint32_t lane0 = (uint32_t)((warp & 3) * 32) << 16;
     const uint32_t aBase = smem_addr(sA), wBase = smem_addr(sW);
+    const int barId = 1 + grp;
     uint32_t phase = 0;
     bool failed = false;
 
     const int tiles = (n + kTcRows - 1) / kTcRows;
-    for (int tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x)
+    for (int tile = blockIdx.x * kInferGroups + grp; tile < tiles && !failed; tile += gridDim.x * kInferGroups)
     {
-        const int q = tile * kTcRows + tid;
+        const int q = tile * kTcRows + row;
         const bool valid = q < n;
-        encode_row(net, queries + (size_t)(valid ? q : 0) * kSampleFloats, valid, sA, tid);
-        float out[48];
+        encode_row_direct(net, queries + (size_t)(valid ? q : 0) * kSampleFloats, valid, sA, row);
         for (int layer = 0; layer < 4; ++layer)
         {
+            // the group's A tile (and, from layer 1, its reads of the accumulator) are complete
             fence_async_smem();
             fence_before_sync();
-            __syncthreads();
-            const uint32_t dcol = (uint32_t)(layer & 1) * 64u;
-            if (tid == 0)
+            group_sync(barId);
+            if (row == 0)
             {
                 fence_after_sync();
                 const uint32_t idesc = instr_desc(kTcRows, layer < 3 ? 64 : kOut);
 #pragma unroll
                 for (int s = 0; s < 4; ++s)
-                    mma_f16(tmem + dcol, smem_desc(aBase + s * 256), smem_desc(wBase + layer * kLayerBytes + s * 256),
-                            idesc, s > 0 ? 1u : 0u);
+                    mma_f16(acc, smem_desc(aBase + s * 256), smem_desc(wBase + layer * kLayerBytes + s * 256), idesc,
+                            s > 0 ? 1u : 0u);
                 mma_commit(mbar);
             }
             const bool ok = mbar_wait(mbar, phase);
             phase ^= 1u;
-            if (__syncthreads_or(!ok))
+            if (group_sync_or(barId, !ok))
             {
-                if (tid == 0) atomicOr(status, LF_DEVERR_GUIDE_TIMEOUT);
+                if (row == 0) atomicOr(status, LF_DEVERR_GUIDE_TIMEOUT);
                 failed = true;
                 break;
             }
             fence_after_sync();
-            if (layer < 3)
+            if (layer == 3) break;   // the outputs stay in TMEM for the epilogue
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
             {
-#pragma unroll
-                for (int c = 0; c < 64; c += 16)
-                {
-                    float v[16];
-                    tmem_ld16(tmem + lane0 + dcol + c, v);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
-                    store8(sA, tid, c, v);
-                    store8(sA, tid, c + 8, v + 8);
-                }
-            }
-            else
-            {
-#pragma unroll
-                for (int c = 0; c < kOut; c += 16) tmem_ld16(tmem + lane0 + dcol + c, out + c);
+                float v[16];
+                tmem_ld16(acc + lane0 + c, v);
                 tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+                store8(sA, row, c, v);
+                store8(sA, row, c + 8, v + 8);
             }
         }
         if (failed) break;
-        if (valid)
+        // epilogue straight from the accumulator: the eight logits first (softmax), then lobe
+        // by lobe its mean and concentration, so that few outputs are live at a time; the TMEM
+        // loads are warp-wide, the stores for valid queries only
+        float e[kLobes];
+#pragma unroll
+        for (int i = 0; i < kLobes; ++i) e[i] = tmem_ld1(acc + lane0 + 5 * i + 4);
+        tmem_wait_ld();
+        float mx = -1e30f;
+#pragma unroll
+        for (int i = 0; i < kLobes; ++i) mx = fmaxf(mx, e[i]);
+        float es = 0.f;
+#pragma unroll
+        for (int i = 0; i < kLobes; ++i)
         {
-            float* dst = mix + (size_t)q * kMixFloats;
-            float mx = -1e30f;
-            for (int i = 0; i < kLobes; ++i) mx = fmaxf(mx, out[5 * i + 4]);
-            float es = 0.f, e[kLobes];
-            for (int i = 0; i < kLobes; ++i)
+            e[i] = __expf(e[i] - mx);
+            es += e[i];
+        }
+        const float invEs = 1.f / es;
+        float* dst = mix + (size_t)(valid ? q : 0) * kMixFloats;
+        float cum = 0.f;
+#pragma unroll
+        for (int i = 0; i < kLobes; ++i)
+        {
+            float o5[4], mu[3], k;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) o5[j] = tmem_ld1(acc + lane0 + 5 * i + j);
+            tmem_wait_ld();
+            lobe_params(o5, mu, &k);
+            cum += e[i] * invEs;
+            if (valid)
             {
-                e[i] = __expf(out[5 * i + 4] - mx);
-                es += e[i];
-            }
-            float cum = 0.f;
-            for (int i = 0; i < kLobes; ++i)
-            {
-                float mu[3], k;
-                lobe_params(out + 5 * i, mu, &k);
-                cum += e[i] / es;
                 dst[5 * i + 0] = mu[0];
                 dst[5 * i + 1] = mu[1];
                 dst[5 * i + 2] = mu[2];
@@ -342,7 +409,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 0)
     {
         fence_after_sync();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tmemSlot), "r"(kTmemCols)
+                     : "memory");
     }
 }
 
@@ -637,11 +705,12 @@ int launch_infer_tc(const Net& net, const float* queries, const int* nDev, int c
     int sms = 1, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // 3 CTAs per SM: the registers (162 per thread) fit 3, shared memory (47 KB) 4, and 3 x 128
-    // TMEM columns stay within the SM's 512, so no allocation waits
+    // kInferCtasPerSm CTAs per SM: the launch bounds cap the registers for that many, shared
+    // memory (about 63 KB per CTA) fits them, and their 3 x 128 TMEM columns stay within the
+    // SM's 512, so no allocation waits
     const int tiles = (cap + kTcRows - 1) / kTcRows;
-    const int blocks = std::max(1, std::min(sms * 3, tiles));
-    guide_infer_tc_kernel<<<blocks, kTcThreads, kTcSmem, st>>>(net, queries, cap, nDev, mix, status);
+    const int blocks = std::max(1, std::min(sms * kInferCtasPerSm, (tiles + kInferGroups - 1) / kInferGroups));
+    guide_infer_tc_kernel<<<blocks, kInferThreads, kTcSmem, st>>>(net, queries, cap, nDev, mix, status);
     return (int)cudaGetLastError();
 }
 }

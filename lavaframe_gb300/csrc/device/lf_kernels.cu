@@ -287,17 +287,20 @@ __global__ void guide_collect_kernel(PathSoA ps, GuideBuffers g, long long n)
             float smp[13];
             if (k < depth - 1)
             {
-                const float* r = g.rec + ((size_t)p * g.maxDepth + k) * kGuideRecFloats;
-                if (r[19] == 2.f && r[12] > 0.f)
+                auto r = [&](int f) { return *guide_rec(g.rec, n, (int)p, k, f); };
+                const float pdf = r(12);
+                if (r(19) == 2.f && pdf > 0.f)
                 {
-                    const float lx = r[13] > 0.f ? (Lf.x - r[16]) / r[13] : 0.f;
-                    const float ly = r[14] > 0.f ? (Lf.y - r[17]) / r[14] : 0.f;
-                    const float lz = r[15] > 0.f ? (Lf.z - r[18]) / r[15] : 0.f;
+                    const float tx = r(13), ty = r(14), tz = r(15);
+                    const float lx = tx > 0.f ? (Lf.x - r(16)) / tx : 0.f;
+                    const float ly = ty > 0.f ? (Lf.y - r(17)) / ty : 0.f;
+                    const float lz = tz > 0.f ? (Lf.z - r(18)) / tz : 0.f;
                     const float lum = 0.2126f * lx + 0.7152f * ly + 0.0722f * lz;
-                    const float w = fminf(lum / r[12], g.weightClamp);
+                    const float w = fminf(lum / pdf, g.weightClamp);
                     if (w > 0.f && w == w)
                     {
-                        for (int c = 0; c < 12; ++c) smp[c] = r[c];
+#pragma unroll
+                        for (int c = 0; c < 12; ++c) smp[c] = r(c);
                         smp[12] = w;
                         take = true;
                     }
@@ -427,7 +430,7 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
     int e = g.tensorPath ? guide::launch_infer_tc(g.net, g.queries, cin, (int)cap, g.mix, b.status, st)
                          : guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
     if (e) return e;
-    GuideCtx gc{g.mix, g.rec, g.alpha, g.maxDepth};
+    GuideCtx gc{g.mix, g.rec, g.alpha, g.maxDepth, cap};
     shade_guided_kernel<<<grid_for((const void*)shade_guided_kernel, B, cap), B, 0, st>>>(
         S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr, gc);
     shadow_kernel<<<grid_for((const void*)shadow_kernel, B, cap), B, 0, st>>>(S, P, ps, b.shadow, b.shadowCount,

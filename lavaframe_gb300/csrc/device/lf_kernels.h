@@ -53,7 +53,7 @@ struct GuideBuffers
     guide::Net net;
     float* queries;      // cap x guide::kSampleFloats
     float* mix;          // cap x guide::kMixFloats
-    float* rec;          // cap x maxDepth x 20, or null when the batch is not recorded
+    float* rec;          // maxDepth x 20 fields x the batch's path slots, or null when the batch is not recorded
     float* train;        // trainCap x guide::kSampleFloats
     int* trainCount;
     int trainCap;

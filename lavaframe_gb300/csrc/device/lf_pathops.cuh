@@ -176,14 +176,22 @@ __device__ __forceinline__ SurfaceGeom surface_geom(const ShadeScene& S, v3 o, v
 // Guided sampling state of one bounce (learned path guiding; no reference counterpart).
 // mix: the mixture of each queue position; rec: per path slot, maxDepth training records of
 // kGuideRecFloats (hit point, outgoing direction, normal, sampled direction, pdf, throughput
-// after the vertex, radiance at the next vertex's start, state).
+// after the vertex, radiance at the next vertex's start, state), stored field-major - field k
+// of vertex d of slot p at (d * kGuideRecFloats + k) * recStride + p - so that a warp's
+// neighbouring slots write and read neighbouring words.
 struct GuideCtx
 {
     const float* mix;
     float* rec;
     float alpha;     // probability of sampling the mixture instead of the BSDF
     int maxDepth;
+    long long recStride;   // path slots of the batch
 };
+
+__device__ __forceinline__ float* guide_rec(float* rec, long long stride, int p, int depth, int k)
+{
+    return rec + ((size_t)depth * kGuideRecFloats + k) * (size_t)stride + p;
+}
 
 // One bounce of PathTrace for the path in slot p after its closest hit is known
 // (pathtrace.glsl:208-294 minus the visibility tests): returns whether the path continues
@@ -213,11 +221,10 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
     {
         // radiance at the start of this vertex: everything the previous vertex's direction
         // has not carried yet
-        float* r = gc.rec + ((size_t)p * gc.maxDepth + depth - 1) * kGuideRecFloats;
-        r[16] = L.x;
-        r[17] = L.y;
-        r[18] = L.z;
-        r[19] = 2.f;
+        *guide_rec(gc.rec, gc.recStride, p, depth - 1, 16) = L.x;
+        *guide_rec(gc.rec, gc.recStride, p, depth - 1, 17) = L.y;
+        *guide_rec(gc.rec, gc.recStride, p, depth - 1, 18) = L.z;
+        *guide_rec(gc.rec, gc.recStride, p, depth - 1, 19) = 2.f;
     }
 
     if (t == kInfinity)
@@ -412,11 +419,11 @@ __device__ __forceinline__ void shade_path_t(const ShadeScene& S, const Params& 
         }
         if (kGuided && gc.rec && depth < gc.maxDepth)
         {
-            float* r = gc.rec + ((size_t)p * gc.maxDepth + depth) * kGuideRecFloats;
             const float vals[16] = {fhp.x, fhp.y, fhp.z, V.x, V.y, V.z, nrm.x, nrm.y, nrm.z,
                                     Ls.x,  Ls.y,  Ls.z,  pdf, T.x, T.y, T.z};
-            for (int k = 0; k < 16; ++k) r[k] = vals[k];
-            r[19] = pushExt ? 1.f : 0.f;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) *guide_rec(gc.rec, gc.recStride, p, depth, k) = vals[k];
+            *guide_rec(gc.rec, gc.recStride, p, depth, 19) = pushExt ? 1.f : 0.f;
         }
         info.y = depth + 1;
         ps.o[p] = f4(o, pdf);
@@ -433,7 +440,7 @@ template <bool kLights = true>
 __device__ __forceinline__ void shade_path(const ShadeScene& S, const Params& P, const PathSoA& ps, int p,
                                            unsigned long long* ctr, bool& pushExt, bool& pushShadow, ShadowRec& rec)
 {
-    shade_path_t<false, kLights>(S, P, ps, p, ctr, pushExt, pushShadow, rec, GuideCtx{nullptr, nullptr, 0.f, 0}, 0);
+    shade_path_t<false, kLights>(S, P, ps, p, ctr, pushExt, pushShadow, rec, GuideCtx{nullptr, nullptr, 0.f, 0, 0}, 0);
 }
 
 // Visibility of a path's next-event rays, then radiance += Li * throughput
