@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--engine-slots", type=int, default=0, help="path slots of the engine pool (0 = default)")
     ap.add_argument("--shade-cap", type=int, default=0, help="engine shade register cap, threads per SM (512/768/1024; 0 = 512)")
     ap.add_argument("--jobs", type=int, default=0, help="serving workload: number of jobs (0 = default)")
-    ap.add_argument("--sort-by-material", action="store_true", help="render workloads: engine sort-by-material")
+    ap.add_argument("--sort-by-material", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="render workloads: engine sort-by-material mode (0 off, 1 on, 2 auto; -1 the default)")
     ap.add_argument("--engine-drain", type=int, default=-1, help="render workloads: engine drain threshold (paths)")
     ap.add_argument("--autotune", action="store_true", help="render workloads: autotune the engine first")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"], help="BVH traversal")
@@ -297,7 +298,10 @@ def c1_reference_image():
     return g["mean"].astype(np.float64), int(g["spp"])
 
 
-def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True, size=None, sort=False):
+def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=True, size=None, sort=None):
+    """One render workload on the engine (or the per-batch pipeline with flags=8). sort: None
+    keeps the engine's sort-by-material mode (default "auto": sorted when the scene mixes
+    material classes), else the mode to render with (0 off, 1 on)."""
     import lavaframe_gb300 as lf
 
     if which == "c1":
@@ -316,8 +320,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
         from lavaframe_gb300 import autotune
 
         tuned = autotune.tune(ctx, ds, p, spp=spp, triangles=int(s.view().num_tris))
-    if sort:
-        ctx.set_engine_sort(True)
+    if sort is not None:
+        ctx.set_engine_sort(sort)
     f = lf.Frame(ctx, ds, p, flags)
     if spp_batch:
         f.set_batch(spp_batch)
@@ -335,7 +339,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
     out = {"Msamples_per_s": ctr[0] / (ms / 1e3) / 1e6, "ext_rays_per_s": ctr[1] / (ms / 1e3),
            "shadow_rays_per_s": ctr[2] / (ms / 1e3), "ms": ms, "ms_runs": runs, "spp": spp,
            "resolution": [p.width, p.height], "max_depth": p.max_depth,
-           "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1]), "sort_by_material": bool(sort)}
+           "triangles": int(s.view().num_tris), "extension_rays": int(ctr[1]),
+           "sort_by_material": "auto" if sort is None else int(sort)}
     if which == "c1" and not size:
         ref = c1_reference_image()
         if ref is not None:
@@ -345,8 +350,8 @@ def render_extra(ctx, which, spp=None, spp_batch=0, flags=0, tune=False, wide=Tr
     if tuned:
         out["autotuned"] = {"config": tuned["config"], "trials": len(tuned["trials"])}
     f.close()
-    if sort:
-        ctx.set_engine_sort(False)
+    if sort is not None:
+        ctx.set_engine_sort("auto")
     ds.close()
     return out
 
@@ -586,7 +591,7 @@ def main():
     if args.workload != "microbench":
         size = tuple(int(x) for x in args.render_size.split("x")) if args.render_size else None
         r = render_extra(ctx, args.workload, spp_batch=args.spp_batch, flags=args.frame_flags,
-                         tune=args.autotune, wide=args.traversal == "wide", size=size, sort=args.sort_by_material)
+                         tune=args.autotune, wide=args.traversal == "wide", size=size, sort=None if args.sort_by_material < 0 else args.sort_by_material)
         if rank == 0:
             print(json.dumps({"metric": f"{args.workload} extension rays/s", "value": r["ext_rays_per_s"],
                               "unit": "rays/s", "detail": r}), flush=True)
@@ -692,7 +697,7 @@ def main():
         if not args.no_extras:
             from lavaframe_gb300 import autotune
 
-            renders = (("c1", "c1", {}), ("c3_1m", "c3", {}), ("c3_1m_sort_by_material", "c3", {"sort": True}),
+            renders = (("c1", "c1", {}), ("c3_1m", "c3", {}), ("c3_1m_unsorted", "c3", {"sort": 0}),
                        ("c3_1m_per_batch", "c3", {"flags": 8}), ("c3_5m", "c3full", {}),
                        ("c3_1m_autotuned", "c3", {"tune": True}))
             for w, which, kw in renders:

@@ -297,9 +297,11 @@ lf_status lf_ctx_configure_engine(lf_ctx* c, int32_t slots, int32_t block_extend
  * fragment where it lands, pathtrace.glsl:246-291): 1 = the extend kernel buckets the paths
  * that hit a surface by the class of their material's shading code (opaque dielectric, metal,
  * transmissive, textured) and shade takes the buckets one after the other, so that a warp
- * runs one class; 0 (default) = hits in the order extend finished them. Results are
- * unchanged either way. The buckets take 16 B per path slot, allocated on first use. Fails
- * with LF_ERR_STATE while passes are in flight. */
+ * runs one class; 0 = hits in the order extend finished them; 2 (default) = sorted in the
+ * steps of a single job whose scene has instances of more than one class, unsorted otherwise
+ * (multi-job steps, single-class scenes). Results are unchanged either way. The buckets take
+ * 16 B per path slot, allocated on first use. Fails with LF_ERR_STATE while passes are in
+ * flight. */
 lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material);
 /* Engine drain threshold (no counterpart in the reference): once every path id of a frame run
  * is issued and at most `paths` paths are still in flight, the run finishes them with one

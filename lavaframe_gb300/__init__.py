@@ -407,8 +407,10 @@ class Context:
 
     def set_engine_sort(self, sort_by_material):
         """Engine sort-by-material: shade takes the paths that hit a surface grouped by the class
-        of their material (results unchanged)."""
-        self._c(lib().lf_ctx_set_engine_sort(self.h, 1 if sort_by_material else 0))
+        of their material (results unchanged). True / 1 on, False / 0 off, "auto" / 2 (default)
+        on for single-job renders of scenes with more than one material class."""
+        mode = 2 if sort_by_material == "auto" else int(sort_by_material)
+        self._c(lib().lf_ctx_set_engine_sort(self.h, mode))
 
     def set_host_chunks(self, chunks=0):
         """Pieces of host-buffer ray queries whose copies overlap tracing (0 = automatic)."""

@@ -18,11 +18,11 @@ CANDIDATES = {
     "shade_threads_per_sm": [0, 512, 768, 1024],
     "block_extend": [64, 128, 256],
     "block_shadow": [64, 128, 256],
-    "sort_by_material": [0, 1],
+    "sort_by_material": [0, 1],   # the default 2 sorts when the scene mixes material classes
     "drain_paths": [1 << 21, 1 << 22, 1 << 23],
 }
 DEFAULT = {"slots": 1 << 24, "shade_threads_per_sm": 512, "block_extend": 128, "block_shadow": 128,
-           "sort_by_material": 0, "drain_paths": 1 << 22}
+           "sort_by_material": 2, "drain_paths": 1 << 22}
 MARGIN = 0.02   # a setting replaces the current one only when it is this much faster (timing noise)
 
 
@@ -33,7 +33,7 @@ def _signature(params, spp, triangles):
 def _apply(ctx, cfg):
     ctx.configure_engine(slots=cfg["slots"], block_extend=cfg["block_extend"], block_shade=128,
                          block_shadow=cfg["block_shadow"], shade_threads_per_sm=cfg["shade_threads_per_sm"])
-    ctx.set_engine_sort(cfg.get("sort_by_material", 0))
+    ctx.set_engine_sort(cfg.get("sort_by_material", 2))
     ctx.set_engine_drain(cfg.get("drain_paths", 1 << 22))
 
 

@@ -55,7 +55,7 @@ lf_status alloc_pool(EngineHost* e, int slots)
     A(&b.done[0], slots);
     A(&b.done[1], slots);
     A(&b.shadow, slots);
-    if (b.sortByMaterial) A(&b.partSort, (size_t)4 * slots);
+    if (e->sortMode == 1) A(&b.partSort, (size_t)4 * slots);
     if (err != cudaSuccess)
     {
         free_engine_buffers(e);
@@ -172,19 +172,39 @@ lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockS
     return LF_OK;
 }
 
-lf_status engine_set_sort(EngineHost* e, bool on)
+namespace
+{
+lf_status ensure_sort_buckets(EngineHost* e)
+{
+    if (e->b.partSort) return LF_OK;
+    size_t bytes = 0;
+    cudaError_t err = dalloc(e->allocs, bytes, &e->b.partSort, (size_t)4 * e->b.cap);
+    if (err != cudaSuccess) return cuda_fail(e->c, err, "sort-by-material buckets");
+    e->poolBytes += bytes;
+    return LF_OK;
+}
+
+// Whether the steps of `one` (nullptr: the multi-job form) sort by material.
+bool sort_on(const EngineHost* e, const EngineJob* one)
+{
+    if (e->sortMode == 1) return true;
+    if (e->sortMode == 0 || !one) return false;
+    const uint32_t m = one->S.shadeClassMask;
+    return (m & (m - 1)) != 0;   // more than one class
+}
+}
+
+lf_status engine_set_sort(EngineHost* e, int mode)
 {
     lf_ctx* c = e->c;
     if (e->active > 0) return fail(c, LF_ERR_STATE, "engine has passes in flight");
     cudaStreamSynchronize(c->stream);
-    if (on && !e->b.partSort)
+    if (mode == 1)
     {
-        size_t bytes = 0;
-        cudaError_t err = dalloc(e->allocs, bytes, &e->b.partSort, (size_t)4 * e->b.cap);
-        if (err != cudaSuccess) return cuda_fail(c, err, "sort-by-material buckets");
-        e->poolBytes += bytes;
+        lf_status st = ensure_sort_buckets(e);
+        if (st != LF_OK) return st;
     }
-    e->b.sortByMaterial = on ? 1 : 0;
+    e->sortMode = mode;
     drop_graphs(e);   // the graphs hold the kernel parameters
     return LF_OK;
 }
@@ -254,9 +274,16 @@ lf_status engine_launch_pair(EngineHost* e, unsigned long long* ctr, int job, bo
     if (!hit)
     {
         if (e->graphs.size() >= 8) drop_graphs(e);
+        const EngineJob* one = job >= 0 ? &e->h_jobStage[job] : nullptr;
+        const bool sort = sort_on(e, one);
+        if (sort)
+        {
+            lf_status st = ensure_sort_buckets(e);
+            if (st != LF_OK) return st;
+        }
         EngineBuffers b = e->b;
         b.ctr = ctr;
-        const EngineJob* one = job >= 0 ? &e->h_jobStage[job] : nullptr;
+        b.sortByMaterial = sort ? 1 : 0;
         cudaGraph_t g = nullptr;
         cudaGraphExec_t exec = nullptr;
         cudaError_t err = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);

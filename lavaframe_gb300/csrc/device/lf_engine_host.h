@@ -34,6 +34,7 @@ struct EngineHost
     };
     std::vector<Graph> graphs;
     long long drainPaths = 1 << 22;     // paths left at which a frame run switches to the drain form (0 = never)
+    int sortMode = 2;                   // sort-by-material: 0 off, 1 on, 2 single-job steps of mixed-class scenes
 };
 
 // Engine of the context, created on first use with the default pool size.
@@ -42,9 +43,10 @@ lf_status engine_get(lf_ctx* c, EngineHost** out);
 // and the register cap of shade (threads per SM it must fit: 0 none, 512, 768, 1024).
 lf_status engine_configure(EngineHost* e, int slots, int blockExtend, int blockShade, int blockShadow,
                            int shadeThreadsPerSm);
-// Sort-by-material on or off: extend buckets the hits by material class (4 x slots queue
-// entries, allocated on first use) and shade takes them class by class.
-lf_status engine_set_sort(EngineHost* e, bool on);
+// Sort-by-material: extend buckets the hits by material class (4 x slots queue entries,
+// allocated on first use) and shade takes them class by class. mode 0 off, 1 on, 2 (default)
+// on for single-job steps whose scene has instances of more than one material class.
+lf_status engine_set_sort(EngineHost* e, int mode);
 int engine_job_alloc(EngineHost* e, const ShadeScene& S, const Params& P);
 void engine_job_write(EngineHost* e, int job, const ShadeScene& S, const Params& P);
 void engine_job_free(EngineHost* e, int job);

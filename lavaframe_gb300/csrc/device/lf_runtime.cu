@@ -534,6 +534,13 @@ void set_bounds(lf_scene* sc, const RefNode& root)
     }
 }
 
+uint32_t shade_class_mask(const std::vector<ShadeInstance>& sinst)
+{
+    uint32_t m = 0;
+    for (const ShadeInstance& s : sinst) m |= 1u << (s.shadeClass & 3);
+    return m;
+}
+
 lf_status encode_instances(lf_ctx* c, const lf_scene_view* v, const RefNode* nodes, std::vector<float4>& recs,
                            std::vector<int>& map, std::vector<float4>& inst, std::vector<ShadeInstance>& sinst,
                            int* tlasRoot)
@@ -764,6 +771,7 @@ lf_status lf_scene_upload(lf_ctx* c, const lf_scene_view* v, lf_scene** out)
     S.materials = d_mats;
     S.inst = d_sinst;
     S.numMaterials = v->num_materials;
+    S.shadeClassMask = shade_class_mask(sinst);
     if (hasEnv)
     {
         S.env.rgb = d_env;
@@ -845,6 +853,7 @@ lf_status lf_scene_update_instances(lf_scene* sc, const lf_scene_view* v)
     sc->view.trav.root = tlasRoot;
     sc->view.trav.numNodes = (int)(recs.size() / 4);
     sc->view.trav.wroot = wroot;
+    sc->view.shadeClassMask = shade_class_mask(sinst);
     set_bounds(sc, nodes[v->top_level_index]);
     return LF_OK;
 }
@@ -1718,13 +1727,13 @@ lf_status lf_ctx_set_engine_drain(lf_ctx* c, int64_t paths)
 
 lf_status lf_ctx_set_engine_sort(lf_ctx* c, int32_t sort_by_material)
 {
-    if (!c || sort_by_material < 0 || sort_by_material > 1) return LF_ERR_INVALID;
+    if (!c || sort_by_material < 0 || sort_by_material > 2) return LF_ERR_INVALID;
     std::lock_guard<std::recursive_mutex> lk(c->mu);
     cudaSetDevice(c->device);
     EngineHost* e = nullptr;
     lf_status st = engine_get(c, &e);
     if (st != LF_OK) return st;
-    return engine_set_sort(e, sort_by_material != 0);
+    return engine_set_sort(e, sort_by_material);
 }
 
 lf_status lf_ctx_engine_info(lf_ctx* c, int64_t* slots, int64_t* device_bytes)

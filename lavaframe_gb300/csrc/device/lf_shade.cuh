@@ -78,6 +78,7 @@ struct ShadeScene
     const DevMaterial* materials;
     const ShadeInstance* inst;
     int numMaterials;
+    uint32_t shadeClassMask;   // bit k: some instance's material has shade class k
     EnvMap env;
     TexArray tex;
 };

@@ -91,16 +91,20 @@ def test_sort_by_material_keeps_results(ctx, slots):
     assert len(classes) >= 2
     try:
         ctx.configure_engine(slots=slots)
+        ctx.set_engine_sort(False)
         base, p = render(ctx, s, 3, size=(64, 36))
         ctx.set_engine_sort(True)
         got, _ = render(ctx, s, 3, size=(64, 36))
+        ctx.set_engine_sort("auto")   # the default: sorted here, the scene mixes classes
+        auto, _ = render(ctx, s, 3, size=(64, 36))
     finally:
-        ctx.set_engine_sort(False)
+        ctx.set_engine_sort("auto")
         ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
                              shade_threads_per_sm=DEFAULT_SHADE_CAP)
-    assert same_bits(got["paths"], base["paths"])
-    assert same_bits(got["accum"], base["accum"])
-    assert got["counters"][1:] == base["counters"][1:]
+    for r in (got, auto):
+        assert same_bits(r["paths"], base["paths"])
+        assert same_bits(r["accum"], base["accum"])
+        assert r["counters"][1:] == base["counters"][1:]
     ref_acc, _, _ = oracle.render(s.view(), p, 0, 3, want_paths=False)
     assert same_bits(got["accum"], ref_acc)
 
