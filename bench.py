@@ -73,7 +73,8 @@ def parse():
     ap.add_argument("--c4-lr", type=float, default=1e-2, help="guiding workload: Adam learning rate")
     ap.add_argument("--c4-tensor", type=int, default=-1,
                     help="guiding workload: MLP on mma.sync (0), tcgen05 (1) or both (-1)")
-    ap.add_argument("--workload", default="microbench", choices=["microbench", "c1", "c3", "c3full", "c4", "c5"],
+    ap.add_argument("--workload", default="microbench",
+                    choices=["microbench", "c1", "c3", "c3full", "c4", "c4batches", "c5"],
                     help="microbench = headline; c1/c3/c3full = one render workload alone (profiling)")
     return ap.parse_args()
 
@@ -552,6 +553,74 @@ def run_guiding(ctx, width, height, ref_spp, plain_spp=1024, batch=16, every=2, 
             "batch": batch, "train_every": every, "alpha": alpha, "lr": lr}
 
 
+def guided_batches(ctx, width, height, batch=16, tensor=1):
+    """Per-sample cost on the occluded-light room of the engine, of the per-batch pipeline and
+    of guided batches (Adam after every second batch), each after its warm-up. One per-batch
+    batch and two guided batches (one that trains, one that does not) run between
+    cuProfilerStart and cuProfilerStop, so that `ncu --profile-from-start off` lists exactly
+    their launches."""
+    import ctypes
+
+    import lavaframe_gb300 as lf
+
+    s = lf.HostScene().gen_room(16700, 4).build()
+    a = s.arrays()
+    top = int(a["top_level_index"])
+    lo, hi = a["nodes"][top][0:3], a["nodes"][top][3:6]
+    p = s.render_params()
+    p.width, p.height = width, height
+    ds = ctx.upload(s)
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        cu = None
+
+    def timed(f, first, n):
+        f.sync()
+        t = time.perf_counter()
+        f.render(first, n)
+        f.sync()
+        return time.perf_counter() - t
+
+    out = {"resolution": [width, height], "batch": batch}
+    f = lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM)
+    f.render(0, batch)
+    out["engine_ms_per_spp"] = timed(f, batch, 4 * batch) / (4 * batch) * 1e3
+    f.close()
+    f = lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM | lf.FRAME_PER_BATCH)
+    f.set_batch(batch)
+    f.render(0, batch)
+    out["per_batch_ms_per_spp"] = timed(f, batch, 4 * batch) / (4 * batch) * 1e3
+    if cu:
+        f.sync()
+        cu.cuProfilerStart()
+        f.render(5 * batch, batch)
+        f.sync()
+        cu.cuProfilerStop()
+    f.close()
+    g = lf.Guide(ctx, lo, hi, seed=1)
+    g.set_tensor_path(bool(tensor))
+    f = lf.Frame(ctx, ds, p, lf.FRAME_FP64_ACCUM)
+    f.set_batch(batch)
+    f.set_guide(g, 0.5, 2, 1e-2)
+    for k in range(8):
+        f.render(k * batch, batch)
+    per = [timed(f, (8 + k) * batch, batch) / batch * 1e3 for k in range(8)]
+    out["guided_ms_per_spp_batches"] = per
+    out["guided_ms_per_spp"] = float(np.mean(per))
+    if cu:
+        f.sync()
+        cu.cuProfilerStart()
+        f.render(16 * batch, batch)
+        f.render(17 * batch, batch)
+        f.sync()
+        cu.cuProfilerStop()
+    f.close()
+    g.close()
+    ds.close()
+    return out
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -579,6 +648,14 @@ def main():
             print(json.dumps({"metric": "c4 guided / plain time to the plain 1024-spp error",
                               "value": r["time_ratio_median"],
                               "unit": "ratio", "higher_is_better": False, "detail": r}), flush=True)
+        ctx.close()
+        return
+    if args.workload == "c4batches":
+        cw, ch = (int(x) for x in args.c4_size.split("x"))
+        r = guided_batches(ctx, cw, ch, tensor=max(args.c4_tensor, 0) if args.c4_tensor >= 0 else 1)
+        if rank == 0:
+            print(json.dumps({"metric": "c4 per-sample cost of plain and guided batches", "value": r["guided_ms_per_spp"],
+                              "unit": "ms/spp", "higher_is_better": False, "detail": r}), flush=True)
         ctx.close()
         return
     if args.workload == "c5":
