@@ -524,6 +524,72 @@ __device__ __noinline__ uint32_t mesh_binary(const DevScene S, int rootCode, int
     return err;
 }
 
+// Two floats in one 64-bit register pair, for the packed f32x2 operations of sm_100 and later:
+// sub.rn.f32x2 / mul.rn.f32x2 round each lane exactly as sub.rn.f32 / mul.rn.f32 do.
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2_dup(float a)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a));
+    return r;
+}
+
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ void f2_split(f2_t v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+
+// Slab distances of the kWide children of a wide node (box_hit_fast's t0 and t1 for each):
+// (bound - o) * invd for two children per packed instruction, then the per-child min / max.
+__device__ __forceinline__ void wide_slabs(const float4* rec, v3 ro, v3 invd, float t0[kWide], float t1[kWide])
+{
+    constexpr int G = kWide / 4;   // float4 per group
+    const f2_t ro2[3] = {f2_dup(ro.x), f2_dup(ro.y), f2_dup(ro.z)};
+    const f2_t iv2[3] = {f2_dup(invd.x), f2_dup(invd.y), f2_dup(invd.z)};
+    ulonglong2 grp[6][G];   // lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the children, two per 64 bits
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+#pragma unroll
+        for (int h4 = 0; h4 < G; ++h4) grp[q][h4] = __ldg(reinterpret_cast<const ulonglong2*>(rec + q * G + h4));
+#pragma unroll
+    for (int h4 = 0; h4 < G; ++h4)
+#pragma unroll
+        for (int half = 0; half < 2; ++half)
+        {
+            float n[3][2], f[3][2];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                const f2_t lo = half ? grp[2 * a][h4].y : grp[2 * a][h4].x;
+                const f2_t hi = half ? grp[2 * a + 1][h4].y : grp[2 * a + 1][h4].x;
+                f2_split(f2_mul(f2_sub(lo, ro2[a]), iv2[a]), n[a][0], n[a][1]);
+                f2_split(f2_mul(f2_sub(hi, ro2[a]), iv2[a]), f[a][0], f[a][1]);
+            }
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+            {
+                const int j = h4 * 4 + half * 2 + c;
+                t1[j] = fmin3_hw(fmaxf(f[0][c], n[0][c]), fmaxf(f[1][c], n[1][c]), fmaxf(f[2][c], n[2][c]));
+                t0[j] = fmax3_hw(fminf(f[0][c], n[0][c]), fminf(f[1][c], n[1][c]), fminf(f[2][c], n[2][c]));
+            }
+        }
+}
+
 // Compare-exchange of two (key, child code) pairs by key: the codes travel with their keys, so
 // no per-slot lookup is needed after the sort.
 __device__ __forceinline__ void sort2(uint32_t& a, uint32_t& b, int& ca, int& cb)
@@ -547,33 +613,27 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
     const float4* rec = S.wnodes + (size_t)code * kWideF4;
     constexpr int G = kWide / 4;   // float4 per group
     constexpr uint32_t kSlotMask = kWide - 1;
-    float g[7][kWide];   // the eighth group (reference indices) is not needed here
-#pragma unroll
-    for (int q = 0; q < 7; ++q)
-#pragma unroll
-        for (int h4 = 0; h4 < G; ++h4)
-        {
-            const float4 f = ldg4(rec + q * G + h4);
-            g[q][h4 * 4 + 0] = f.x;
-            g[q][h4 * 4 + 1] = f.y;
-            g[q][h4 * 4 + 2] = f.z;
-            g[q][h4 * 4 + 3] = f.w;
-        }
+    float t0[kWide], t1[kWide];
+    wide_slabs(rec, ro, invd, t0, t1);
     uint32_t key[kWide];
     int child[kWide];
+#pragma unroll
+    for (int h4 = 0; h4 < G; ++h4)
+    {
+        const int4 c = __ldg(reinterpret_cast<const int4*>(rec + 6 * G + h4));
+        child[h4 * 4 + 0] = c.x;
+        child[h4 * 4 + 1] = c.y;
+        child[h4 * 4 + 2] = c.z;
+        child[h4 * 4 + 3] = c.w;
+    }
     int nh = 0;
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
     {
         // box_hit_fast's value is > 0 exactly when t1 >= t0 and t1 > 0; NaN boxes fail both
-        const float fx = (g[1][j] - ro.x) * invd.x, fy = (g[3][j] - ro.y) * invd.y, fz = (g[5][j] - ro.z) * invd.z;
-        const float nx = (g[0][j] - ro.x) * invd.x, ny = (g[2][j] - ro.y) * invd.y, nz = (g[4][j] - ro.z) * invd.z;
-        const float t1 = fmin3_hw(fmaxf(fx, nx), fmaxf(fy, ny), fmaxf(fz, nz));
-        const float t0 = fmax3_hw(fminf(fx, nx), fminf(fy, ny), fminf(fz, nz));
-        const float e = fmaxf(t0, 0.f);
-        const bool hit = t1 >= t0 && t1 > 0.f && e <= lim;
+        const float e = fmaxf(t0[j], 0.f);
+        const bool hit = t1[j] >= t0[j] && t1[j] > 0.f && e <= lim;
         key[j] = hit ? ((__float_as_uint(e) & ~kSlotMask) | (uint32_t)j) : 0xFFFFFFFFu;
-        child[j] = __float_as_int(g[6][j]);
         nh += hit ? 1 : 0;
     }
 #define LF_S2(a, b) sort2(key[a], key[b], child[a], child[b])
@@ -615,38 +675,34 @@ __device__ __forceinline__ int wide_node_any(const DevScene& S, int code, v3 ro,
 {
     const float4* rec = S.wnodes + (size_t)code * kWideF4;
     constexpr int G = kWide / 4;
-    float g[7][kWide];
-#pragma unroll
-    for (int q = 0; q < 7; ++q)
-#pragma unroll
-        for (int h4 = 0; h4 < G; ++h4)
-        {
-            const float4 f = ldg4(rec + q * G + h4);
-            g[q][h4 * 4 + 0] = f.x;
-            g[q][h4 * 4 + 1] = f.y;
-            g[q][h4 * 4 + 2] = f.z;
-            g[q][h4 * 4 + 3] = f.w;
-        }
+    float t0[kWide], t1[kWide];
+    wide_slabs(rec, ro, invd, t0, t1);
     bool hit[kWide];
     int nh = 0;
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
     {
-        const float fx = (g[1][j] - ro.x) * invd.x, fy = (g[3][j] - ro.y) * invd.y, fz = (g[5][j] - ro.z) * invd.z;
-        const float nx = (g[0][j] - ro.x) * invd.x, ny = (g[2][j] - ro.y) * invd.y, nz = (g[4][j] - ro.z) * invd.z;
-        const float t1 = fmin3_hw(fmaxf(fx, nx), fmaxf(fy, ny), fmaxf(fz, nz));
-        const float t0 = fmax3_hw(fminf(fx, nx), fminf(fy, ny), fminf(fz, nz));
-        hit[j] = t1 >= t0 && t1 > 0.f && fmaxf(t0, 0.f) <= lim;
+        hit[j] = t1[j] >= t0[j] && t1[j] > 0.f && fmaxf(t0[j], 0.f) <= lim;
         nh += hit[j] ? 1 : 0;
     }
     if (sp + nh - 1 > kWideStack) return kWideEmpty;
+    int child[kWide];
+#pragma unroll
+    for (int h4 = 0; h4 < G; ++h4)
+    {
+        const int4 c = __ldg(reinterpret_cast<const int4*>(rec + 6 * G + h4));
+        child[h4 * 4 + 0] = c.x;
+        child[h4 * 4 + 1] = c.y;
+        child[h4 * 4 + 2] = c.z;
+        child[h4 * 4 + 3] = c.w;
+    }
     int next = kWideNone;
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
         if (hit[j])
         {
             if (next != kWideNone) stack[sp++] = next;
-            next = __float_as_int(g[6][j]);
+            next = child[j];
         }
     return next;
 }
