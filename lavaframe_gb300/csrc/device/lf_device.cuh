@@ -554,18 +554,28 @@ __device__ __forceinline__ void f2_split(f2_t v, float& a, float& b)
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
 
-// Slab distances of the kWide children of a wide node (box_hit_fast's t0 and t1 for each):
-// (bound - o) * invd for two children per packed instruction, then the per-child min / max.
+// Slab distances of the kWide children of a wide node (box_hit_fast's t0 and t1 for each),
+// for a ray whose inverse direction is finite and non-zero: (bound - o) * invd for two children
+// per packed instruction. On an axis with invd > 0 the lower bound's distance is the smaller of
+// the two (lo <= hi, and subtracting o and multiplying by a positive number keep the order), on
+// an axis with invd < 0 the upper bound's: the bounds are read in near / far order for the
+// ray's octant, and box_hit_fast's per-axis min / max reduce to t0 = max(near) and
+// t1 = min(far) with the same values (unused slots hold NaN boxes, which give NaN either way).
 __device__ __forceinline__ void wide_slabs(const float4* rec, v3 ro, v3 invd, float t0[kWide], float t1[kWide])
 {
     constexpr int G = kWide / 4;   // float4 per group
     const f2_t ro2[3] = {f2_dup(ro.x), f2_dup(ro.y), f2_dup(ro.z)};
     const f2_t iv2[3] = {f2_dup(invd.x), f2_dup(invd.y), f2_dup(invd.z)};
-    ulonglong2 grp[6][G];   // lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the children, two per 64 bits
+    const int neg[3] = {invd.x < 0.f ? 1 : 0, invd.y < 0.f ? 1 : 0, invd.z < 0.f ? 1 : 0};
+    ulonglong2 nearB[3][G], farB[3][G];   // per axis the near and far bounds, two children per 64 bits
 #pragma unroll
-    for (int q = 0; q < 6; ++q)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int h4 = 0; h4 < G; ++h4) grp[q][h4] = __ldg(reinterpret_cast<const ulonglong2*>(rec + q * G + h4));
+        for (int h4 = 0; h4 < G; ++h4)
+        {
+            nearB[a][h4] = __ldg(reinterpret_cast<const ulonglong2*>(rec + (2 * a + neg[a]) * G + h4));
+            farB[a][h4] = __ldg(reinterpret_cast<const ulonglong2*>(rec + (2 * a + 1 - neg[a]) * G + h4));
+        }
 #pragma unroll
     for (int h4 = 0; h4 < G; ++h4)
 #pragma unroll
@@ -575,8 +585,8 @@ __device__ __forceinline__ void wide_slabs(const float4* rec, v3 ro, v3 invd, fl
 #pragma unroll
             for (int a = 0; a < 3; ++a)
             {
-                const f2_t lo = half ? grp[2 * a][h4].y : grp[2 * a][h4].x;
-                const f2_t hi = half ? grp[2 * a + 1][h4].y : grp[2 * a + 1][h4].x;
+                const f2_t lo = half ? nearB[a][h4].y : nearB[a][h4].x;
+                const f2_t hi = half ? farB[a][h4].y : farB[a][h4].x;
                 f2_split(f2_mul(f2_sub(lo, ro2[a]), iv2[a]), n[a][0], n[a][1]);
                 f2_split(f2_mul(f2_sub(hi, ro2[a]), iv2[a]), f[a][0], f[a][1]);
             }
@@ -584,8 +594,8 @@ __device__ __forceinline__ void wide_slabs(const float4* rec, v3 ro, v3 invd, fl
             for (int c = 0; c < 2; ++c)
             {
                 const int j = h4 * 4 + half * 2 + c;
-                t1[j] = fmin3_hw(fmaxf(f[0][c], n[0][c]), fmaxf(f[1][c], n[1][c]), fmaxf(f[2][c], n[2][c]));
-                t0[j] = fmax3_hw(fminf(f[0][c], n[0][c]), fminf(f[1][c], n[1][c]), fminf(f[2][c], n[2][c]));
+                t1[j] = fmin3_hw(f[0][c], f[1][c], f[2][c]);
+                t0[j] = fmax3_hw(n[0][c], n[1][c], n[2][c]);
             }
         }
 }
