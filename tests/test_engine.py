@@ -109,6 +109,31 @@ def test_sort_by_material_keeps_results(ctx, slots):
     assert same_bits(got["accum"], ref_acc)
 
 
+def test_depth_zero_job_is_black_and_matches_oracle(ctx):
+    """A job of depth 0: its paths go from the refill straight to the done list and the finish
+    kernel writes out zero radiance; no ray is traced. Small pools keep the step kernels running."""
+    s = icospheres()
+    try:
+        ctx.configure_engine(slots=1024)
+        p = s.render_params()
+        p.width, p.height = 48, 27
+        p.max_depth = 0
+        ds = ctx.upload(s)
+        f = lf.Frame(ctx, ds, p)
+        f.render(0, 3)
+        f.sync()
+        acc, ctr = f.accum(), f.counters()
+        f.close()
+        ds.close()
+    finally:
+        ctx.configure_engine(slots=DEFAULT_SLOTS, block_extend=0, block_shade=0, block_shadow=0,
+                             shade_threads_per_sm=DEFAULT_SHADE_CAP)
+    ref_acc, _, ref_ctr = oracle.render(s.view(), p, 0, 3, want_paths=False)
+    assert same_bits(acc, ref_acc)
+    assert not acc.any()
+    assert ctr[1] == 0 and ref_ctr[1] == 0
+
+
 @pytest.mark.parametrize("drain", [0, 1 << 10, 1 << 24])
 def test_drain_threshold_keeps_results(ctx, drain):
     """The run's switch to the one-kernel drain (never, late, or from the first step) changes

@@ -82,6 +82,34 @@ def test_jobs_in_a_mix_equal_jobs_alone(ctx, paths_per_pass):
         assert got[k].tobytes() == frame_alone(ctx, s, p, spp).tobytes(), k
 
 
+def test_depth_zero_job_beside_regular_jobs(ctx):
+    """Multi-job steps with a job of depth 0 among regular ones: its paths are written out by
+    the finish kernel (black image) while the others' images stay those they have alone."""
+    cornell = scenes.build("cornell")
+    ico = lf.HostScene().gen_icospheres(6, 3, 5, 64, 32).build()
+    zero = ico.render_params()
+    zero.width, zero.height, zero.max_depth = 40, 24, 0
+    reg = cornell.render_params()
+    reg.width, reg.height = 48, 32
+    reg2 = ico.render_params()
+    reg2.width, reg2.height = 40, 24
+    srv = lf.Server(ctx, paths_per_pass=1500, passes_per_job=2)
+    try:
+        sc, si = srv.add_scene(cornell), srv.add_scene(ico)
+        jobs = [(srv.submit(si, zero, 3), ico, zero, 3), (srv.submit(sc, reg, 3), cornell, reg, 3),
+                (srv.submit(si, reg2, 2), ico, reg2, 2)]
+        got = []
+        for jid, _, _, _ in jobs:
+            assert srv.wait(jid, 60000)
+            got.append(srv.read(jid))
+            srv.release(jid)
+    finally:
+        srv.close()
+    assert not got[0].any()
+    for img, (_, s, p, spp) in zip(got[1:], jobs[1:]):
+        assert img.tobytes() == frame_alone(ctx, s, p, spp).tobytes()
+
+
 def test_budget_evicts_idle_scenes_least_recently_used(ctx):
     """A budget that holds the engine pool and one scene at a time: alternating scenes
     upload and evict, and every result stays exact."""
