@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffe
             freeOff[buf][lane] = off;
             if (lane == 0)
             {
-                // ids handed out so far: this round's share, or a look at the counter
+                // ids handed out so far: the share of this block's scan step, or a look at the counter
                 const int rb = atomicAdd(&ctl->refillNext, tot);
                 roundBase[buf] = rb;
                 if constexpr (kOne)
