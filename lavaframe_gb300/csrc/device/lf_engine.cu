@@ -172,7 +172,7 @@ __global__ void engine_reset_kernel(EngineCtl* c, int parity)
 // ------------------------------------------------------------------ finish / refill
 constexpr int kFinishUnroll = 4;   // done entries a thread has in flight
 constexpr int kRefillBlock = 256;  // refill block size (8 warps)
-constexpr int kRefillGroups = 4;   // groups of kRefillBlock slots a refill block takes per round
+constexpr int kRefillGroups = 4;   // groups of kRefillBlock slots a refill block takes per scan step
 
 // Writes out the radiance of the paths on the done list (paths of depth-0 jobs; the step
 // kernels end every other path where it ends), counting pass completions, and frees their
@@ -227,12 +227,12 @@ __device__ __forceinline__ int warp_exclusive_scan(int& v)
 }
 
 // Starts min(free slots, unissued ids) new paths in free slots taken in slot order: the pool is
-// scanned in rounds of kRefillGroups x kRefillBlock slots per block, a round's free slots get
+// scanned in steps of kRefillGroups x kRefillBlock slots per block, a step's free slots get
 // consecutive ids (next + k for the k-th slot handed out, in slot order), each new path gets
 // its camera ray (renderer.glsl:27-62) and is queued for extension in the same order (a
 // depth-0 job's paths go straight to the done list with zero radiance). Handing out slots in
 // slot order keeps the paths a warp shades in neighbouring slots, so their state comes in few
-// cache lines, however the earlier paths finished. One round takes two block barriers (four
+// cache lines, however the earlier paths finished. One scan step takes two block barriers (four
 // for a multi-job pool) and one atomic per counter.
 template <bool kOne>
 __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffers b, EngineJob one, int parity)
@@ -240,12 +240,12 @@ __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffe
     constexpr int kG = kRefillGroups;
     constexpr int kW = kRefillBlock / 32;
     static_assert(kG * kW == 32, "one scan entry per lane of a warp");
-    // double-buffered by round, so that a round needs no barrier at its end
+    // double-buffered by scan step, so that a step needs no barrier at its end
     __shared__ unsigned freeMask[2][32];   // per (group, warp): free slots, then
-    __shared__ int freeOff[2][32];         // their exclusive offsets in the round
+    __shared__ int freeOff[2][32];         // their exclusive offsets in the scan step
     __shared__ int runOff[2][2][32];       // multi-job pool: queued / done offsets per (group, warp)
     __shared__ unsigned runMask[2][2][32];
-    __shared__ int roundBase[2], queueBase[2], doneBase[2];
+    __shared__ int stepBase[2], queueBase[2], doneBase[2];
     EngineCtl* ctl = b.ctl;
     const unsigned long long next = ctl->next, total = ctl->total;
     const int freeCount = ctl->freeCount;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffe
             {
                 // ids handed out so far: the share of this block's scan step, or a look at the counter
                 const int rb = atomicAdd(&ctl->refillNext, tot);
-                roundBase[buf] = rb;
+                stepBase[buf] = rb;
                 if constexpr (kOne)
                 {
                     const int got = rb < m ? (tot < m - rb ? tot : m - rb) : 0;
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffe
             }
         }
         __syncthreads();
-        const int rb = roundBase[buf];
+        const int rb = stepBase[buf];
         if (rb >= m) break;   // every id of this step is handed out
         int slotOf[kG];
         unsigned runBits = 0;
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kRefillBlock) engine_refill_kernel(EngineBuffe
         {
             slotOf[g] = -1;
             const unsigned fm = freeMask[buf][g * kW + warp];
-            const int r = freeOff[buf][g * kW + warp] + __popc(fm & below);   // rank in the round
+            const int r = freeOff[buf][g * kW + warp] + __popc(fm & below);   // rank in the scan step
             const int k = rb + r;
             if (((fm >> lane) & 1u) && k < m)
             {
