@@ -57,12 +57,14 @@ def test_engine_equals_per_batch_pipeline(ctx, name, flags):
     assert eng["counters"][1:] == ref["counters"][1:]   # extension rays, shadow rays, clamps
 
 
-def test_small_pool_regenerates_and_matches_oracle(ctx):
-    """1024 slots for 4608 paths: most slots run several paths; partial edge tiles."""
+@pytest.mark.parametrize("slots", [1024, 1000])
+def test_small_pool_regenerates_and_matches_oracle(ctx, slots):
+    """1024 slots for 4608 paths: most slots run several paths; partial edge tiles. 1000 slots:
+    a pool that the refill's 1024-slot scan steps do not divide."""
     s = icospheres()
     try:
-        ctx.configure_engine(slots=1024)
-        assert ctx.engine_info()["slots"] == 1024
+        ctx.configure_engine(slots=slots)
+        assert ctx.engine_info()["slots"] == slots
         got, p = render(ctx, s, 2, size=(64, 36), tile=(20, 12), first=1)
         ref_acc, _, ctr = oracle.render(s.view(), p, 1, 2, want_paths=False)
         assert same_bits(got["accum"], ref_acc)
