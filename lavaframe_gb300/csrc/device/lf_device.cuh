@@ -54,7 +54,8 @@ struct DevLight
 // Wide nodes collapsed from the reference's binary tree (see traverse_wide): per node
 // 2 * kWide float4 = [min x | max x | min y | max y | min z | max z | child codes | child
 // reference-node indices], kWide values per group (kWide / 4 float4 each); unused slots have
-// code kWideEmpty and a NaN box (no slab test passes it). The width is a build option
+// code kWideEmpty and the empty box lo = +inf, hi = -inf (no slab test passes it: wide_slabs
+// reads it as entry +inf, exit -inf). The width is a build option
 // (LF_WIDE = 4 or 8).
 #ifndef LF_WIDE
 #define LF_WIDE 4
@@ -560,7 +561,9 @@ __device__ __forceinline__ void f2_split(f2_t v, float& a, float& b)
 // the two (lo <= hi, and subtracting o and multiplying by a positive number keep the order), on
 // an axis with invd < 0 the upper bound's: the bounds are read in near / far order for the
 // ray's octant, and box_hit_fast's per-axis min / max reduce to t0 = max(near) and
-// t1 = min(far) with the same values (unused slots hold NaN boxes, which give NaN either way).
+// t1 = min(far) with the same values. An unused slot's empty box (lo = +inf, hi = -inf) gives
+// t0 = +inf and t1 = -inf for every such ray: (+inf - o) * invd and (-inf - o) * invd are
+// +inf and -inf in near / far order whatever the sign of invd.
 __device__ __forceinline__ void wide_slabs(const float4* rec, v3 ro, v3 invd, float t0[kWide], float t1[kWide])
 {
     constexpr int G = kWide / 4;   // float4 per group
@@ -640,9 +643,13 @@ __device__ __forceinline__ int wide_node(const DevScene& S, int code, v3 ro, v3 
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
     {
-        // box_hit_fast's value is > 0 exactly when t1 >= t0 and t1 > 0; NaN boxes fail both
-        const float e = fmaxf(t0[j], 0.f);
-        const bool hit = t1[j] >= t0[j] && t1[j] > 0.f && e <= lim;
+        // box_hit_fast's value is > 0 exactly when t1 >= t0 and t1 > 0, and the entry
+        // max(t0, 0) must not exceed lim (> 0). With e = max(t0, smallest positive float) the
+        // three tests are one, e <= min(t1, lim): for t0 > 0, e = t0; for t0 <= 0 it asks
+        // t1 > 0 (lim > 0 always). e's bits differ from max(t0, 0)'s only below the key's slot
+        // bits. An unused slot (t0 = +inf, t1 = -inf) fails.
+        const float e = fmaxf(t0[j], 1.401298464e-45f);
+        const bool hit = e <= fminf(t1[j], lim);
         key[j] = hit ? ((__float_as_uint(e) & ~kSlotMask) | (uint32_t)j) : 0xFFFFFFFFu;
         nh += hit ? 1 : 0;
     }
@@ -692,7 +699,7 @@ __device__ __forceinline__ int wide_node_any(const DevScene& S, int code, v3 ro,
 #pragma unroll
     for (int j = 0; j < kWide; ++j)
     {
-        hit[j] = t1[j] >= t0[j] && t1[j] > 0.f && fmaxf(t0[j], 0.f) <= lim;
+        hit[j] = fmaxf(t0[j], 1.401298464e-45f) <= fminf(t1[j], lim);   // as in wide_node
         nh += hit[j] ? 1 : 0;
     }
     if (sp + nh - 1 > kWideStack) return kWideEmpty;

@@ -389,9 +389,10 @@ lf_status wide_level(lf_ctx* c, WideBuilder& B, int start, bool meshLevel, int* 
         for (int j = 0; j < kWide; ++j)
         {
             int code = kWideEmpty, refIdx = -1;
-            // an unused slot gets a NaN box, which no slab test passes
-            const float qnan = std::numeric_limits<float>::quiet_NaN();
-            float lo[3] = {qnan, qnan, qnan}, hi[3] = {qnan, qnan, qnan};
+            // an unused slot gets the empty box lo = +inf, hi = -inf: read in near / far order
+            // (wide_slabs) its entry is +inf and its exit -inf for every ray, so no test passes
+            const float inf = std::numeric_limits<float>::infinity();
+            float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
             if (j < (int)kids.size())
             {
                 const int k = kids[j];
