@@ -217,14 +217,19 @@ __global__ void trace_any_kernel(DevScene S, const float4* rays, long long n, ui
 // ------------------------------------------------------------------ guided bounces
 // Query record (position, outgoing direction, shading normal) of every queued path that hit a
 // triangle; other entries get a zero record (their mixture is computed and not used).
-__global__ void guide_query_kernel(ShadeScene S, PathSoA ps, const int* queue, const int* qcount, float* queries)
+// pixelShare > 0 (the first bounce of a batch of several samples): one query per pixel, from the
+// pixel's sample-0 path (slot p < pixelShare), stored at the pixel's index; the other queued
+// paths write none.
+__global__ void guide_query_kernel(ShadeScene S, PathSoA ps, const int* queue, const int* qcount, float* queries,
+                                   int pixelShare)
 {
     const int n = *qcount;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const int p = queue[i];
+        if (pixelShare > 0 && p >= pixelShare) continue;
         const float4 h = ps.hit[p];
-        float* q = queries + (size_t)i * guide::kSampleFloats;
+        float* q = queries + (size_t)(pixelShare > 0 ? p : i) * guide::kSampleFloats;
         float v[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 1.f};
         const int prim = __float_as_int(h.z), light = __float_as_int(h.w);
         if (h.x != kInfinity && light < 0 && prim >= 0)
@@ -238,10 +243,12 @@ __global__ void guide_query_kernel(ShadeScene S, PathSoA ps, const int* queue, c
     }
 }
 
+// pixelShare > 0: the mixtures are per pixel (guide_query_kernel's pixelShare), path p uses its
+// pixel's, p % pixelShare.
 __global__ void __launch_bounds__(128, 4) shade_guided_kernel(ShadeScene S, Params P, PathSoA ps, const int* qin,
                                                                const int* qinCount, int* qout, int* qoutCount,
                                                                ShadowRec* sq, int* sqCount, int cap, uint32_t* status,
-                                                               unsigned long long* ctr, GuideCtx gc)
+                                                               unsigned long long* ctr, GuideCtx gc, int pixelShare)
 {
     const int n = *qinCount;
     const int stride = gridDim.x * blockDim.x;
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(128, 4) shade_guided_kernel(ShadeScene S, Para
         if (i < n)
         {
             p = qin[i];
-            shade_path_t<true>(S, P, ps, p, ctr, pushExt, pushShadow, rec, gc, i);
+            shade_path_t<true>(S, P, ps, p, ctr, pushExt, pushShadow, rec, gc, pixelShare > 0 ? p % pixelShare : i);
         }
         warp_push(pushExt, p, qout, qoutCount, cap, status);
         warp_push(pushShadow, rec, sq, sqCount, cap, status);
@@ -426,13 +433,21 @@ int launch_bounce_guided(const ShadeScene& S, const Params& P, const PathSoA& ps
     cudaMemsetAsync(b.fetch, 0, 2 * sizeof(unsigned long long), st);
     extend_kernel<<<grid_for((const void*)extend_kernel, B, cap), B, 0, st>>>(S, P, ps, qin, cin, b.fetch, b.status,
                                                                               b.ctr);
-    guide_query_kernel<<<grid_for((const void*)guide_query_kernel, B, cap), B, 0, st>>>(S, ps, qin, cin, g.queries);
-    int e = g.tensorPath ? guide::launch_infer_tc(g.net, g.queries, cin, (int)cap, g.mix, b.status, st)
-                         : guide::launch_infer(g.net, g.queries, cin, (int)cap, g.mix, st);
+    // First bounce of a batch of several samples: the samples of a pixel hit its footprint
+    // from the same camera, so they share one mixture, inferred from the pixel's sample-0 path
+    // (a proposal that does not depend on the other samples' own draws keeps them unbiased).
+    const long long tilePix = (long long)P.tileW * P.tileH;
+    const int share = bounce == 0 && cap > tilePix ? (int)tilePix : 0;
+    guide_query_kernel<<<grid_for((const void*)guide_query_kernel, B, cap), B, 0, st>>>(S, ps, qin, cin, g.queries,
+                                                                                      share);
+    const int* nq = share ? nullptr : cin;
+    const int qcap = share ? share : (int)cap;
+    int e = g.tensorPath ? guide::launch_infer_tc(g.net, g.queries, nq, qcap, g.mix, b.status, st)
+                         : guide::launch_infer(g.net, g.queries, nq, qcap, g.mix, st);
     if (e) return e;
     GuideCtx gc{g.mix, g.rec, g.alpha, g.maxDepth, cap};
     shade_guided_kernel<<<grid_for((const void*)shade_guided_kernel, B, cap), B, 0, st>>>(
-        S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr, gc);
+        S, P, ps, qin, cin, qout, cout, b.shadow, b.shadowCount, (int)cap, b.status, b.ctr, gc, share);
     shadow_kernel<<<grid_for((const void*)shadow_kernel, B, cap), B, 0, st>>>(S, P, ps, b.shadow, b.shadowCount,
                                                                              b.fetch + 1, b.status, b.ctr);
     return (int)cudaGetLastError();
